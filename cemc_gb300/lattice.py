@@ -1,0 +1,444 @@
+"""FCC supercells, cluster enumeration and the settings object a CE updater reads.
+
+The reference takes its lattice, clusters, translation matrix and basis
+functions from a CLEASE settings object (``BC``) and parses it in
+``cpp/src/ce_updater.cpp:43-212`` and ``cpp/src/cluster.cpp:185-232``.  CLEASE is
+not part of this project, so this module generates the same information for
+face-centred-cubic supercells from the geometry alone:
+
+* sites of an ``L x L x L`` conventional cubic supercell (4 sites per cube),
+  ordered like ``bulk(..., cubic=True).repeat((L, L, L))``;
+* neighbour shells and all pair / triplet / quadruplet clusters that contain
+  the reference site 0, classified into symmetry-distinct types with the 48
+  operations of the cubic point group plus lattice translations;
+* for every sub-cluster the ``order`` permutation onto a canonical labelling
+  and, per type, the ``equiv_sites`` groups (orbits of the cluster's own
+  symmetry), which fix the equivalent-decoration averaging of
+  ``cpp/src/cluster.cpp:41-128``;
+* the translation table ``T[i, c]`` = site reached from site ``i`` by the
+  offset of neighbour column ``c`` (the reference's
+  ``RowSparseStructMatrix``, ``cpp/src/row_sparse_struct_matrix.cpp:114-122``);
+* basis functions: binary spins (+1, -1) and the ternary basis
+  phi1 = sqrt(3/2) s, phi2 = sqrt(2) (1 - 3/2 s^2) over spins (+1, 0, -1).
+
+Cluster names follow the reference's naming contract: ``c0``, ``c1_<d>`` and
+``c<size>_d<dia>_<variant>_<decostring>``; the decoration string is the part
+after the last underscore (``ce_updater.cpp:701-710``).
+"""
+from __future__ import annotations
+
+import itertools
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Sequence, Tuple
+
+import numpy as np
+
+# Conventional FCC basis in half-lattice-constant units.
+_FCC_BASIS = np.array([(0, 0, 0), (0, 1, 1), (1, 0, 1), (1, 1, 0)], dtype=np.int64)
+_BASIS_INDEX = {(0, 0, 0): 0, (0, 1, 1): 1, (1, 0, 1): 2, (1, 1, 0): 3}
+
+
+def _cubic_point_group() -> np.ndarray:
+    """The 48 signed permutation matrices of the cubic group O_h."""
+    ops = []
+    for perm in itertools.permutations(range(3)):
+        for signs in itertools.product((1, -1), repeat=3):
+            m = np.zeros((3, 3), dtype=np.int64)
+            for r, (c, s) in enumerate(zip(perm, signs)):
+                m[r, c] = s
+            ops.append(m)
+    return np.array(ops)
+
+
+_OH = _cubic_point_group()
+
+
+def fcc_shell_vectors(max_shell: int) -> List[np.ndarray]:
+    """Neighbour vectors of the FCC lattice (half-lattice units), one array per shell.
+
+    Shell k (1-based) holds every lattice vector with the k-th smallest
+    non-zero length.  FCC lattice vectors are the integer vectors whose
+    coordinate sum is even.
+    """
+    r = 2
+    while True:
+        rng = np.arange(-r, r + 1)
+        g = np.array(np.meshgrid(rng, rng, rng, indexing="ij")).reshape(3, -1).T
+        g = g[(g.sum(axis=1) % 2 == 0) & (np.abs(g).sum(axis=1) > 0)]
+        d2 = (g * g).sum(axis=1)
+        radii = np.unique(d2)
+        # Every shell up to max_shell is complete if its radius is below r^2.
+        if len(radii) >= max_shell and radii[max_shell - 1] < r * r:
+            shells = []
+            for k in range(max_shell):
+                v = g[d2 == radii[k]]
+                order = np.lexsort(v.T[::-1])
+                shells.append(v[order])
+            return shells
+        r += 1
+
+
+def shell_radius2(max_shell: int) -> List[int]:
+    return [int((s[0] * s[0]).sum()) for s in fcc_shell_vectors(max_shell)]
+
+
+@dataclass
+class ClusterType:
+    """One symmetry-distinct cluster (the reference's ``Cluster``, ``cluster.hpp:14-54``)."""
+
+    name: str  # prefix, e.g. c2_d0000_0
+    size: int
+    dia2: int  # squared max distance, half-lattice units
+    prototype: np.ndarray  # (size, 3) canonical labelling of the sites
+    equiv_sites: List[List[int]]
+    # Sub-clusters containing the reference site (site at the origin):
+    offsets: List[np.ndarray] = field(default_factory=list)  # (size-1, 3) member vectors
+    order: List[List[int]] = field(default_factory=list)  # canonical position -> index in [ref]+members
+
+
+def _canonical_key(points: np.ndarray) -> Tuple:
+    """Symmetry-invariant key of a finite point set (translations + O_h)."""
+    best = None
+    for v in points:
+        shifted = points - v
+        for g in _OH:
+            img = shifted @ g.T
+            key = tuple(sorted(map(tuple, img.tolist())))
+            if best is None or key < best:
+                best = key
+    return best
+
+
+def _map_onto(points: np.ndarray, proto: np.ndarray) -> List[int]:
+    """Find a lattice symmetry carrying ``proto`` onto ``points``.
+
+    Returns ``order`` with ``order[q]`` = index into ``points`` of the site that
+    canonical position ``q`` lands on.
+    """
+    proto_set = {tuple(p): q for q, p in enumerate(proto.tolist())}
+    for v in points:
+        shifted = points - v
+        for g in _OH:
+            img = shifted @ g.T
+            mapping = [proto_set.get(tuple(p)) for p in img.tolist()]
+            if None in mapping or len(set(mapping)) != len(mapping):
+                continue
+            order = [0] * len(points)
+            for idx, q in enumerate(mapping):
+                order[q] = idx
+            return order
+    raise RuntimeError("sub-cluster is not equivalent to its prototype")
+
+
+def _equiv_sites(proto: np.ndarray) -> List[List[int]]:
+    """Orbits (size >= 2) of the prototype's own symmetry on its positions."""
+    n = len(proto)
+    parent = list(range(n))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    proto_set = {tuple(p): q for q, p in enumerate(proto.tolist())}
+    for v in proto:
+        shifted = proto - v
+        for g in _OH:
+            img = shifted @ g.T
+            # translate so that the image coincides with the prototype as a set
+            for w in proto:
+                cand = img + w
+                mapping = [proto_set.get(tuple(p)) for p in cand.tolist()]
+                if None in mapping or len(set(mapping)) != n:
+                    continue
+                for q in range(n):
+                    a, b = find(q), find(mapping[q])
+                    if a != b:
+                        parent[a] = b
+    groups: Dict[int, List[int]] = {}
+    for q in range(n):
+        groups.setdefault(find(q), []).append(q)
+    return [sorted(gq) for gq in sorted(groups.values()) if len(gq) >= 2]
+
+
+def enumerate_cluster_types(pair_shells: int, triplet_shells: int, quad_shells: int) -> List[ClusterType]:
+    """All pair/triplet/quad types of the FCC lattice with max distance in the given shells.
+
+    A cluster of size >= 3 belongs to the set if every pairwise distance is at
+    most the radius of shell ``triplet_shells`` (resp. ``quad_shells``); size 0
+    means "no clusters of that size".
+    """
+    max_shell = max(pair_shells, triplet_shells, quad_shells, 1)
+    shells = fcc_shell_vectors(max_shell)
+    radii = [int((s[0] * s[0]).sum()) for s in shells]
+    types: List[ClusterType] = []
+
+    def add_size(size: int, n_shells: int):
+        if n_shells <= 0:
+            return
+        cutoff = radii[n_shells - 1]
+        nbrs = np.concatenate(shells[:n_shells])
+        found: Dict[Tuple, ClusterType] = {}
+        for combo in itertools.combinations(range(len(nbrs)), size - 1):
+            pts = np.vstack([np.zeros((1, 3), dtype=np.int64), nbrs[list(combo)]])
+            diff = pts[:, None, :] - pts[None, :, :]
+            d2 = (diff * diff).sum(axis=2)
+            if d2.max() > cutoff:
+                continue
+            key = _canonical_key(pts)
+            ct = found.get(key)
+            if ct is None:
+                proto = np.array(key, dtype=np.int64)
+                ct = ClusterType(name="", size=size, dia2=int(d2.max()), prototype=proto,
+                                 equiv_sites=_equiv_sites(proto))
+                found[key] = ct
+            ct.offsets.append(pts[1:].copy())
+            ct.order.append(_map_onto(pts, ct.prototype))
+        # Name: c<size>_d<dia index>_<variant>, diameters ranked within this size.
+        cts = sorted(found.values(), key=lambda c: (c.dia2, len(c.offsets), c.prototype.tolist()))
+        dias = sorted({c.dia2 for c in cts})
+        variant: Dict[int, int] = {}
+        for c in cts:
+            di = dias.index(c.dia2)
+            v = variant.get(di, 0)
+            variant[di] = v + 1
+            c.name = "c%d_d%04d_%d" % (size, di, v)
+            types.append(c)
+
+    add_size(2, pair_shells)
+    add_size(3, triplet_shells)
+    add_size(4, quad_shells)
+    return types
+
+
+def equivalent_decorations(deco: Sequence[int], equiv_sites: Sequence[Sequence[int]]) -> List[List[int]]:
+    """Distinct decorations reachable by permuting positions inside each equivalent-site group.
+
+    This is the averaging set the reference obtains from
+    ``equivalent_deco`` (called at ``cpp/src/cluster.cpp:78-110``): the product of
+    the permutation groups of every group of equivalent positions, applied to
+    the decoration, with duplicates removed (first occurrence kept).
+    """
+    deco = list(deco)
+    if not equiv_sites:
+        return [deco]
+    per_group = [list(itertools.permutations(g)) for g in equiv_sites]
+    out: List[List[int]] = []
+    seen = set()
+    for choice in itertools.product(*per_group):
+        new = list(deco)
+        for group, perm in zip(equiv_sites, choice):
+            for src, dst in zip(group, perm):
+                new[dst] = deco[src]
+        t = tuple(new)
+        if t not in seen:
+            seen.add(t)
+            out.append(new)
+    return out
+
+
+def binary_basis(symbols: Sequence[str]) -> List[Dict[str, float]]:
+    """Spin basis for two species: +1 for the first (sorted) symbol, -1 for the second."""
+    s = sorted(symbols)
+    return [{s[0]: 1.0, s[1]: -1.0}]
+
+
+def ternary_basis(symbols: Sequence[str]) -> List[Dict[str, float]]:
+    """phi1 = sqrt(3/2) s, phi2 = sqrt(2) (1 - 1.5 s^2), spins +1, 0, -1 in sorted symbol order."""
+    s = sorted(symbols)
+    spins = {s[0]: 1.0, s[1]: 0.0, s[2]: -1.0}
+    phi1 = {k: math.sqrt(1.5) * v for k, v in spins.items()}
+    phi2 = {k: math.sqrt(2.0) * (1.0 - 1.5 * v * v) for k, v in spins.items()}
+    return [phi1, phi2]
+
+
+class FCCSupercell:
+    """Sites and periodic translation of an ``L x L x L`` conventional FCC supercell."""
+
+    def __init__(self, L: int, a: float = 4.05):
+        if L < 1:
+            raise ValueError("supercell size must be positive")
+        self.L = int(L)
+        self.a = float(a)
+        self.period = 2 * self.L
+        cells = np.array(list(itertools.product(range(L), repeat=3)), dtype=np.int64)
+        pos = (2 * cells)[:, None, :] + _FCC_BASIS[None, :, :]
+        self.positions = pos.reshape(-1, 3)  # half-lattice units
+        self.n_sites = len(self.positions)
+
+    def index_of(self, pos: np.ndarray) -> np.ndarray:
+        """Site index of (possibly unwrapped) positions, shape (..., 3)."""
+        p = np.mod(pos, self.period)
+        cell = p // 2
+        parity = p % 2
+        b = np.zeros(p.shape[:-1], dtype=np.int64)
+        b[(parity == (0, 1, 1)).all(-1)] = 1
+        b[(parity == (1, 0, 1)).all(-1)] = 2
+        b[(parity == (1, 1, 0)).all(-1)] = 3
+        valid = ((parity == (0, 0, 0)).all(-1) | (b > 0))
+        if not np.all(valid):
+            raise ValueError("position is not an FCC lattice site")
+        L = self.L
+        return ((cell[..., 0] * L + cell[..., 1]) * L + cell[..., 2]) * 4 + b
+
+
+@dataclass
+class ECIName:
+    name: str
+    kind: str  # "c0", "c1" or "cluster"
+    decoration: List[int]
+    cluster: int = -1  # index into ClusterSet.types for kind == "cluster"
+
+
+class ClusterSet:
+    """Cluster types, decorations and ECI names of one lattice/cluster recipe."""
+
+    def __init__(self, types: List[ClusterType], n_bf: int):
+        self.types = types
+        self.n_bf = n_bf
+        self.type_index = {t.name: i for i, t in enumerate(types)}
+        names: List[ECIName] = [ECIName("c0", "c0", [])]
+        for b in range(n_bf):
+            names.append(ECIName("c1_%d" % b, "c1", [b]))
+        for ti, t in enumerate(types):
+            reps = set()
+            for deco in itertools.product(range(n_bf), repeat=t.size):
+                eq = equivalent_decorations(deco, t.equiv_sites)
+                rep = min(tuple(d) for d in eq)
+                reps.add(rep)
+            for rep in sorted(reps):
+                s = "".join(str(d) for d in rep)
+                names.append(ECIName("%s_%s" % (t.name, s), "cluster", list(rep), ti))
+        # NamedArray keeps its names sorted (cpp/src/named_array.cpp:7-23).
+        names.sort(key=lambda e: e.name)
+        self.eci_names = names
+
+    @property
+    def names(self) -> List[str]:
+        return [e.name for e in self.eci_names]
+
+    def neighbour_offsets(self) -> np.ndarray:
+        """Distinct member offsets over all sub-clusters (the table columns), sorted."""
+        offs = set()
+        for t in self.types:
+            for o in t.offsets:
+                for v in o.tolist():
+                    offs.add(tuple(v))
+        return np.array(sorted(offs), dtype=np.int64).reshape(-1, 3)
+
+
+def fcc_cluster_set(pair_shells: int, triplet_shells: int, quad_shells: int, n_species: int) -> ClusterSet:
+    return ClusterSet(enumerate_cluster_types(pair_shells, triplet_shells, quad_shells), n_species - 1)
+
+
+class Settings:
+    """Duck-typed stand-in for the settings object ``CEUpdater::init`` reads.
+
+    Attribute formats follow ``cpp/src/ce_updater.cpp:43-212`` and
+    ``cpp/src/cluster.cpp:185-232``: ``unique_elements``, ``num_unique_elements``,
+    ``index_by_trans_symm``, ``background_indices``, ``cluster_info``,
+    ``basis_functions`` and ``trans_matrix`` (here a list of dicts, the
+    reference's sparse form, since the dense form is ``N x max_column``).
+    It also carries the packed arrays the GPU path uses.
+    """
+
+    def __init__(self, cell: FCCSupercell, cset: ClusterSet, symbols: Sequence[str]):
+        self.cell = cell
+        self.cset = cset
+        self.unique_elements = sorted(symbols)
+        self.num_unique_elements = len(self.unique_elements)
+        if self.num_unique_elements - 1 != cset.n_bf:
+            raise ValueError("cluster set decorations do not match the species count")
+        if self.num_unique_elements == 2:
+            self.basis_functions = binary_basis(self.unique_elements)
+        elif self.num_unique_elements == 3:
+            self.basis_functions = ternary_basis(self.unique_elements)
+        else:
+            raise ValueError("only binary and ternary alloys are generated")
+        n = cell.n_sites
+        self.n_sites = n
+        self.index_by_trans_symm = [list(range(n))]
+        self.background_indices: List[int] = []
+        offs = cset.neighbour_offsets()
+        self.column_offsets = offs
+        col_sites = cell.index_of(offs)  # site index of each column = neighbour of site 0
+        if len(set(col_sites.tolist())) != len(col_sites) or 0 in set(col_sites.tolist()):
+            raise ValueError("supercell too small: neighbour offsets alias onto the same site")
+        self.column_sites = col_sites
+        # table[i, c] = site reached from site i by column offset c
+        self.table = cell.index_of(cell.positions[:, None, :] + offs[None, :, :]).astype(np.int32)
+        off_to_col = {tuple(v): c for c, v in enumerate(offs.tolist())}
+        self.member_cols: List[np.ndarray] = []
+        info: Dict[str, dict] = {}
+        for t in cset.types:
+            cols = np.array([[off_to_col[tuple(v)] for v in o.tolist()] for o in t.offsets], dtype=np.int32)
+            self.member_cols.append(cols)
+            indices = [[int(col_sites[c]) for c in row] for row in cols]
+            info[t.name] = {
+                "ref_indx": 0,
+                "size": t.size,
+                "max_cluster_dia": 0.5 * cell.a * math.sqrt(t.dia2),
+                "symm_group": 0,
+                "name": t.name,
+                "descriptor": "fcc_%d_body_d2_%d" % (t.size, t.dia2),
+                "indices": indices,
+                "order": [list(o) for o in t.order],
+                "equiv_sites": [list(g) for g in t.equiv_sites],
+            }
+        self.cluster_info = [info]
+        self._trans_list = None
+
+    @property
+    def trans_matrix(self):
+        """Sparse translation matrix: one dict ``{column site: site}`` per row."""
+        if self._trans_list is None:
+            cols = self.column_sites.tolist()
+            self._trans_list = [dict(zip(cols, row)) for row in self.table.tolist()]
+        return self._trans_list
+
+    def symbol_ids(self, symbols: Sequence[str]) -> np.ndarray:
+        lut = {s: i for i, s in enumerate(self.unique_elements)}
+        return np.array([lut[s] for s in symbols], dtype=np.int8)
+
+    def bf_table(self) -> np.ndarray:
+        """bf[b, id] as in ``cpp/src/basis_function.cpp:5-19``."""
+        out = np.zeros((len(self.basis_functions), self.num_unique_elements))
+        for b, d in enumerate(self.basis_functions):
+            for s, v in d.items():
+                out[b, self.unique_elements.index(s)] = v
+        return out
+
+
+def fcc_settings(L: int, pair_shells: int, triplet_shells: int, quad_shells: int,
+                 symbols: Sequence[str], a: float = 4.05) -> Settings:
+    cset = fcc_cluster_set(pair_shells, triplet_shells, quad_shells, len(symbols))
+    return Settings(FCCSupercell(L, a), cset, symbols)
+
+
+def seeded_ecis(cset: ClusterSet, seed: int, c0: float = -3.0, singlet_sigma: float = 0.05,
+                pair_sigma: float = 0.02, triplet_sigma: float = 0.005, quad_sigma: float = 0.002) -> Dict[str, float]:
+    """ECIs drawn as in the benchmark recipes.
+
+    c0 fixed; singlets N(0, singlet_sigma); pairs N(0, pair_sigma / shell) where
+    shell is the 1-based neighbour shell of the pair; triplets and quadruplets
+    N(0, sigma).  Drawn in sorted-name order from ``numpy.random.default_rng(seed)``.
+    """
+    rng = np.random.default_rng(seed)
+    eci: Dict[str, float] = {}
+    for e in cset.eci_names:
+        if e.kind == "c0":
+            eci[e.name] = float(c0)
+        elif e.kind == "c1":
+            eci[e.name] = float(rng.normal(0.0, singlet_sigma))
+        else:
+            t = cset.types[e.cluster]
+            if t.size == 2:
+                shell = int(t.name.split("_")[1][1:]) + 1
+                eci[e.name] = float(rng.normal(0.0, pair_sigma / shell))
+            elif t.size == 3:
+                eci[e.name] = float(rng.normal(0.0, triplet_sigma))
+            else:
+                eci[e.name] = float(rng.normal(0.0, quad_sigma))
+    return eci

@@ -1,0 +1,183 @@
+/* C ABI of the GB300 cluster-expansion Monte Carlo library (libcemc_gb300.so).
+ *
+ * Every entry point returns int status (0 = OK, never throws, never traps);
+ * the message of the last failure on the calling thread is available from
+ * cemc_last_error().  Device buffers are owned by the caller (PyTorch tensors
+ * on the Python side) and passed as raw pointers plus a cudaStream_t (void*).
+ * The only allocation the library makes is the device copy of a geometry's
+ * tables in cemc_geometry_create().
+ *
+ * The entry points replace the reference's native CE updater,
+ * cpp/include/ce_updater.hpp:47-213 (class CEUpdater), as bound by
+ * cemc/cpp_ext/pyce_updater.pyx:5-60 (PyCEUpdater).  Each declaration names
+ * the reference member it stands in for.
+ */
+#ifndef CEMC_GB300_H
+#define CEMC_GB300_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CEMC_OK 0
+#define CEMC_ERR_ARG 1        /* invalid argument (sizes, null pointers) */
+#define CEMC_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define CEMC_ERR_BACKGROUND 3 /* attempted to move a background site (ce_updater.cpp:330-332) */
+#define CEMC_ERR_STATE 4      /* move inconsistent with the current occupation (ce_updater.cpp:530-537) */
+#define CEMC_ERR_LIMIT 5      /* a compiled-in limit was exceeded */
+#define CEMC_ERR_TIMEOUT 6    /* a bounded device wait ran out */
+
+#define CEMC_MAX_BF 4         /* decorations per site (species - 1) */
+#define CEMC_MAX_ECI 128      /* ECIs per cluster expansion */
+#define CEMC_MAX_COLS 128     /* distinct neighbour columns per site */
+
+/* Running sums a chain accumulates after every trial (accepted or not).
+ * Energies are taken relative to e_ref to keep the squares well conditioned;
+ * the reference keeps the same sums in Averager objects and SGCObserver
+ * (cemc/mcmc/montecarlo.py:802-814, cemc/mcmc/mc_observers.py:222-271). */
+typedef struct {
+  double e_ref;                  /* energy offset of the sums below */
+  double sum_e;                  /* sum of (E - e_ref) */
+  double sum_e2;                 /* sum of (E - e_ref)^2 */
+  double sum_s[CEMC_MAX_BF];     /* sum of singlet correlation functions */
+  double sum_s2[CEMC_MAX_BF];    /* sum of squared singlets */
+  double sum_se[CEMC_MAX_BF];    /* sum of singlet * (E - e_ref) */
+  uint64_t n_samples;            /* trials accumulated */
+  uint64_t n_accept;             /* accepted trials */
+} cemc_accum;
+
+/* Host description of one supercell geometry and cluster expansion.  All
+ * arrays are host memory; cemc_geometry_create() copies them to the device.
+ * Layout of the flattened cluster "terms" (one per sub-cluster and
+ * equivalent decoration of a cluster ECI):
+ *   term_eci[t]   ECI index the term contributes to
+ *   term_ref[t]   decoration index applied to the changed site
+ *   term_size[t]  cluster size (2..4)
+ *   term_nb[t*3+j] packed (column * n_bf + decoration) of member j
+ * Terms are sorted by ECI; eci_weight[k] = size / (|eq deco| * M_k * N_s)
+ * is the reference's increment normalisation (ce_updater.cpp:400-402). */
+typedef struct {
+  int32_t n_sites;        /* N, including background sites */
+  int32_t n_cols;         /* neighbour columns per site */
+  int32_t n_sym;          /* species */
+  int32_t n_bf;           /* decorations = n_sym - 1 */
+  int32_t n_eci;          /* ECIs, sorted-name order */
+  int32_t n_terms;        /* flattened cluster terms */
+  const int32_t *table;   /* [n_sites * n_cols] neighbour site of (site, column) */
+  const double *bf;       /* [n_bf * n_sym] basis function values */
+  const int32_t *eci_kind;   /* [n_eci] 0 = c0, 1 = singlet, 2 = cluster */
+  const int32_t *eci_dec;    /* [n_eci] decoration of a singlet, else -1 */
+  const double *eci_weight;  /* [n_eci] increment weight of cluster ECIs */
+  const double *eci_full_weight; /* [n_eci] full-recompute weight (weight / size) */
+  const int32_t *term_eci;   /* [n_terms] */
+  const int32_t *term_ref;   /* [n_terms] */
+  const int32_t *term_size;  /* [n_terms] */
+  const int32_t *term_nb;    /* [n_terms * 3] */
+} cemc_geometry_desc;
+
+typedef struct cemc_geometry cemc_geometry;
+
+/* Build the device-resident tables of one geometry (replaces the table
+ * parsing in CEUpdater::init, ce_updater.cpp:32-234). */
+int cemc_geometry_create(const cemc_geometry_desc *desc, cemc_geometry **out);
+int cemc_geometry_destroy(cemc_geometry *geo);
+
+/* Ensembles of a trial move. */
+#define CEMC_MOVE_FLIP 0  /* semi-grand-canonical single-site flip (sgc_montecarlo.py:62-76) */
+#define CEMC_MOVE_SWAP 1  /* canonical two-site swap (montecarlo.py:890-908) */
+
+/* Precision of the trial-move energy change. */
+#define CEMC_PREC_F64 0
+#define CEMC_PREC_F32 1
+
+/* Per-launch description of a batch of chains sharing one geometry.  All
+ * pointers are device memory laid out chain-major.
+ *   occ      [n_chains * n_sites] int8 species ids (sorted-symbol order)
+ *   cf       [n_chains * n_eci]   FP64 correlation functions
+ *   energy   [n_chains]           FP64 total energy N * sum(eci * cf)
+ *   eci      [n_chains * n_eci]   FP64 ECIs (chemical potentials folded in)
+ *   kT       [n_chains]           FP64 k_B * T in eV
+ *   trial    [n_chains]           uint64 first trial index (RNG counter), advanced by n_trials
+ *   accum    [n_chains]           running sums, may be NULL
+ *   trk/loc  [n_chains * n_sites] per-species site lists of swap moves (NULL for flips)
+ *   trk_start[n_chains * n_sym], trk_count [n_chains * n_sym] list extents (NULL for flips)
+ * Optional per-trial trace (device, n_chains * n_trials entries, NULL = off):
+ *   trace_site [.. * 2] int32 sites, trace_acc int8 decision, trace_de FP64 energy change. */
+typedef struct {
+  int32_t n_chains;
+  int32_t move;        /* CEMC_MOVE_* */
+  int32_t precision;   /* CEMC_PREC_* */
+  int32_t warps;       /* warps per chain (trials evaluated per round); 0 = default */
+  uint64_t seed;
+  uint64_t n_trials;   /* trials per chain in this launch */
+  int8_t *occ;
+  double *cf;
+  double *energy;
+  const double *eci;
+  const double *kT;
+  uint64_t *trial;
+  cemc_accum *accum;
+  int32_t *trk;
+  int32_t *loc;
+  const int32_t *trk_start;
+  const int32_t *trk_count;
+  int32_t *trace_site;
+  int8_t *trace_acc;
+  double *trace_de;
+  int32_t *status;     /* [n_chains] device status words, may be NULL */
+} cemc_run_desc;
+
+/* Run n_trials Metropolis trials on every chain in one launch: trial-move
+ * energy change, accept test and in-place commit of occupation, correlation
+ * functions and energy (replaces the Montecarlo._mc_step loop,
+ * montecarlo.py:970-1038, over CEUpdater::calculate / undo_changes /
+ * clear_history, ce_updater.cpp:313-555). */
+int cemc_run(const cemc_geometry *geo, const cemc_run_desc *run, void *stream);
+
+/* Full correlation-function recompute over all sites of every chain, used for
+ * validation and to reset FP64 drift; also rewrites energy = N * eci . cf.
+ * The reference obtains these from ase.clease CorrFunction.get_cf
+ * (cemc/ce_calculator.py:169-177).  scratch: device FP64 buffer of
+ * cemc_recompute_scratch_doubles() entries. */
+size_t cemc_recompute_scratch_doubles(const cemc_geometry *geo, int32_t n_chains);
+int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
+                   double *cf, double *energy, double *scratch, void *stream);
+
+/* Apply an explicit list of single-site changes in sequence to one chain
+ * (CEUpdater::calculate / update_cf, ce_updater.cpp:313-406, 471-519, 845-853):
+ * sites[i] takes species new_sym[i]; cf and energy are updated in place.
+ * old_sym[i] must match the current species or CEMC_ERR_STATE is returned
+ * through *status.  Device pointers; status is a device int32. */
+int cemc_apply_changes(const cemc_geometry *geo, int8_t *occ, double *cf, double *energy, const double *eci,
+                       int32_t n_changes, const int32_t *sites, const int8_t *old_sym, const int8_t *new_sym,
+                       int32_t *status, void *stream);
+
+/* Energy change of a single flip or a swap without committing it (the
+ * replay / debug path).  move: CEMC_MOVE_FLIP uses (site_a, new_a);
+ * CEMC_MOVE_SWAP exchanges the species of site_a and site_b.  Writes the
+ * FP64 energy change and the correlation-function change (n_eci) to device
+ * memory. */
+int cemc_delta_e(const cemc_geometry *geo, const int8_t *occ, const double *eci, int32_t move, int32_t site_a,
+                 int32_t site_b, int32_t new_a, double *de_out, double *dcf_out, void *stream);
+
+/* Replica exchange over a ladder of chains (ParallelTempering
+ * _perform_exchange_move, cemc/mcmc/parallel_tempering.py:138-175): pairs
+ * (i, i+1) of ladder positions starting at parity `direction`, accepted when
+ * u < exp((1/kT_i - 1/kT_j)(E_i - E_j)).  Temperatures are exchanged, not
+ * configurations: replica_of[pos] names the chain at ladder position pos and
+ * is permuted in place; kT[chain] is rewritten accordingly. */
+int cemc_pt_exchange(int32_t n_replicas, int32_t direction, uint64_t seed, uint64_t round,
+                     const double *energy, double *kT, int32_t *replica_of, int32_t *n_accept, void *stream);
+
+/* Message of the last failure on this thread. */
+int cemc_last_error(char *buf, size_t len);
+
+/* Library version and the compute capability it was compiled for. */
+int cemc_version(int32_t *major, int32_t *minor, int32_t *sm);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
