@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""Headline benchmark: Monte Carlo trials/s of the batched semi-grand-canonical workload.
+
+Workload (one GPU): binary FCC alloy, 16x16x16 conventional supercell (16384
+sites, periodic), clusters c0, singlet, pairs to the 4th shell, triplets to
+the 2nd shell, the nearest-neighbour tetrahedron; seeded ECIs (c0 = -3 eV,
+singlet N(0, 0.05), pairs N(0, 0.02/shell), triplets N(0, 0.005), quadruplets
+N(0, 0.002)); 64 independent chains on an 8 x 8 grid of T in [300, 1200] K x
+mu in [-0.2, 0.2] eV (mu folded into c1_0); single-site flips; energy changes
+in FP32, running energy / correlation functions in FP64 with a full FP64
+recompute after every step.  One step = 100 sweeps of every chain
+(64 x 100 x 16384 trials) in one persistent launch plus the recompute,
+replayed from a CUDA graph; 20 steps are the full 2000-sweep budget.
+
+``--impl reference`` times the CPU restatement of the reference's updater and
+Metropolis loop on the host cores instead (the reference tree is not present
+where this runs, so its compiled updater is not available; the restatement is
+bit-identical to it on the pinned fixtures).
+
+Multi-GPU (torchrun, one rank per GPU): independent replicas, no data-path
+collective; the barrier and the max-over-ranks timing are the only collectives.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC trials/sec, batched FP32-dE vs plain GPU vs CPU ref; job p50/p99 latency"
+UNIT = "trials/s"
+KB = 8.6173303e-5
+L_CELL = 16
+N_CHAINS = 64
+SWEEPS_PER_STEP = 100
+SHELLS = (4, 2, 1)
+SPECIES = ["Al", "Mg"]
+BYTES_PER_FLIP = None  # 5 * n_cols + 1, set from the model
+
+
+def workload(seed_offset: int = 0):
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    from cemc_gb300.batch import sgc_grid, fold_chemical_potential
+    s = fcc_settings(L_CELL, *SHELLS, SPECIES)
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    rng = np.random.default_rng(seed_offset)
+    occ = np.zeros((N_CHAINS, m.n_sites), dtype=np.int8)
+    half = m.n_sites // 2
+    for c in range(N_CHAINS):
+        occ[c, rng.permutation(m.n_sites)[:half]] = 1  # 50/50 random initial configuration
+    Ts, mus = sgc_grid()
+    ev = fold_chemical_potential(m, m.eci_vector(eci), mus)
+    return s, m, occ, ev, Ts
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world: int, backend: str):
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend=backend)
+        return dist
+    return None
+
+
+def max_over_ranks(value: float, dist, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value: float, dist, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        import tempfile
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [p.strip() for p in line.split(",")]
+                    if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                        rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": sorted(reasons),
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3] not in ("", "[N/A]"))}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the MC kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "mc_kernel_sgc_64x16384.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_port_rate(m, occ, ev, Ts, sample_sweeps: float, threads: int, seed: int = 7):
+    """Trials/s of the CPU restatement of the reference path over a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    orc = O.Oracle(m)
+    states = [orc.new_chain_state(occ[c], ev[c], KB * Ts[c], O.MOVE_FLIP) for c in range(len(occ))]
+    n_trials = max(1, int(sample_sweeps * m.n_sites))
+    t0 = time.perf_counter()
+    orc.run_many(states, seed=seed, chain_ids=list(range(len(occ))), t_begin=0, n_trials=n_trials,
+                 n_threads=threads)
+    dt = time.perf_counter() - t0
+    return len(occ) * n_trials / dt, n_trials, dt
+
+
+def calibrated_cpu_sample(m, occ, ev, Ts, threads: int, target_s: float):
+    rate, _, _ = cpu_port_rate(m, occ, ev, Ts, 0.02, threads)
+    sweeps = max(0.02, target_s * rate / (len(occ) * m.n_sites))
+    return sweeps
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0  # the CPU arm runs on rank 0 only
+    s, m, occ, ev, Ts = workload(0)
+    threads = os.cpu_count() or 1
+    sweeps = calibrated_cpu_sample(m, occ, ev, Ts, threads, target_s=max(1.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_port_rate(m, occ, ev, Ts, sweeps, threads)
+    total_trials, total_t = 0, 0.0
+    for k in range(args.steps):
+        r, n, dt = cpu_port_rate(m, occ, ev, Ts, sweeps, threads, seed=100 + k)
+        total_trials += N_CHAINS * n
+        total_t += dt
+    value = total_trials / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sgc_flip_fcc_binary_16x16x16_64chains", "n_sites": m.n_sites,
+                   "n_chains": N_CHAINS, "sample_sweeps_per_step": sweeps, "l2": "cpu run"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "%d chains x %.3f sweeps per step of the same workload on %d host threads "
+                                   "(C restatement of the reference CEUpdater + Metropolis loop)"
+                                   % (N_CHAINS, sweeps, threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    dist = init_dist(world, "nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cemc_gb300 import engine as E
+    from cemc_gb300.batch import BatchRunner
+    from cemc_gb300.calculator import model_and_geometry
+
+    s, m, occ, ev, Ts = workload(rank)
+    geo = E.Geometry(m, dev)
+    bytes_per_flip = 5 * m.n_cols + 1
+    keys = np.arange(N_CHAINS) + rank * N_CHAINS
+    runner = BatchRunner(geo, occ, ev, Ts, E.MOVE_FLIP, seed=2026, precision=E.PREC_F32, warps=args.warps,
+                         sweeps_per_step=SWEEPS_PER_STEP, recompute_every=1, graph=True, chain_keys=keys)
+    stream = runner.stream
+    runner.capture()
+    trials_per_step = N_CHAINS * runner.trials_per_step
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+
+    for _ in range(args.warmup):
+        runner.step()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush_l2()
+            ev_s[k].record(stream)
+            runner.step()
+            ev_e[k].record(stream)
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    dev_ms = sum(a.elapsed_time(b) for a, b in zip(ev_s, ev_e))
+    t_max = max_over_ranks(dev_ms * 1e-3, dist, dev)
+    total_trials = sum_over_ranks(float(trials_per_step * args.steps), dist, dev)
+    value = total_trials / t_max
+    clocks = clk.summary()
+    thermo = runner.thermodynamics()
+
+    # -- roofline of the dominant kernel: the MC launch alone, timed on its stream --------
+    cb = runner.cb
+    kms = []
+    for _ in range(3):
+        flush_l2()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            cb.run(runner.trials_per_step, precision=E.PREC_F32, warps=runner.warps)
+            b.record(stream)
+        stream.synchronize()
+        kms.append(a.elapsed_time(b))
+    k_ms = statistics.median(kms)
+    alg_bytes = bytes_per_flip * trials_per_step
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = profiled_traffic()
+
+    # -- end to end through the public batched API, host buffers each step ---------------
+    occ_h = torch.from_numpy(occ).pin_memory()
+    eci_h = torch.from_numpy(np.ascontiguousarray(ev)).pin_memory()
+    kT_h = torch.from_numpy(KB * Ts).pin_memory()
+    n_out = N_CHAINS * (E.ACCUM_DOUBLES + m.n_eci + 1)
+    out_h = torch.empty(n_out, dtype=torch.float64).pin_memory()
+    occ_out_h = torch.empty_like(occ_h).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        runner.load_state(occ_h, eci_h, kT_h)
+        runner.step()
+        with torch.cuda.stream(stream):
+            packed = torch.cat([cb.accum.reshape(-1), cb.cf.reshape(-1), cb.energy.reshape(-1)])
+            out_h.copy_(packed, non_blocking=True)
+            occ_out_h.copy_(cb.occ, non_blocking=True)
+        stream.synchronize()
+    e2e_t = max_over_ranks(time.perf_counter() - t0, dist, dev)
+    e2e_value = sum_over_ranks(float(trials_per_step * e2e_steps), dist, dev) / e2e_t
+    h2d = occ_h.numel() + eci_h.numel() * 8 + kT_h.numel() * 8
+    d2h = n_out * 8 + occ_out_h.numel()
+
+    # -- plain GPU form: one chain per launch, FP64, one sweep per launch, no graph ------
+    plain = None
+    if rank == 0:
+        pb = E.ChainBatch(geo, occ[:1], ev[:1], KB * Ts[:1], E.MOVE_FLIP, seed=5)
+        pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_launch = 4
+        for _ in range(n_launch):
+            pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps)
+        torch.cuda.synchronize()
+        plain = n_launch * m.n_sites / (time.perf_counter() - t0)
+
+    # -- CPU baseline on a bounded sample (rank 0) --------------------------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sweeps = calibrated_cpu_sample(m, occ, ev, Ts, threads, target_s=args.cpu_seconds)
+        rate, n, dt = cpu_port_rate(m, occ, ev, Ts, sweeps, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "%d chains x %.3f sweeps (%.1f s) of the same workload on %d host threads "
+                         "(C restatement of the reference CEUpdater + Metropolis loop)"
+                         % (N_CHAINS, sweeps, dt, threads)}
+
+    if rank == 0:
+        n_launches = 3 * args.steps  # per step: the MC kernel and the two recompute kernels
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "sgc_flip_fcc_binary_16x16x16_64chains", "n_sites": m.n_sites,
+                       "n_chains": N_CHAINS, "sweeps_per_step": SWEEPS_PER_STEP, "recompute": "fp64 every step",
+                       "warps_per_chain": runner.warps, "cuda_graph": True,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
+            "gpu_launches": n_launches,
+            "clocks": clocks,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "mc_kernel<float, flip>", "kernel_ms": k_ms,
+                         "alg_bytes_per_trial": bytes_per_flip},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "plain_gpu": {"value": plain, "unit": UNIT,
+                          "form": "one chain per launch, FP64 energy change, one sweep per launch, no graph"},
+            "cpu_baseline": cpu,
+            "thermo_sample": {"chain0": thermo[0], "chain63": thermo[-1]},
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--warps", type=int, default=0, help="warps per chain (0 = autotuned)")
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args(argv)
+    if args.warmup < 3:
+        p.error("at least 3 warm-up steps")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

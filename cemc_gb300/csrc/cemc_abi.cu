@@ -1,0 +1,383 @@
+// C ABI of libcemc_gb300.so (declared in include/cemc_gb300.h).
+//
+// Host-side work here: validating descriptors, packing a geometry's cluster
+// terms into the per-lane chunks the kernels walk, sizing shared memory and
+// launching.  No entry point throws; failures return a status code and leave a
+// message for cemc_last_error().
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cemc_kernels.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(CEMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct cemc_geometry {
+  cemc::DevGeo g;
+  void *dev = nullptr;  // one device allocation holding every table
+  int max_smem = 0;     // opt-in shared memory per block of the current device
+};
+
+extern "C" int cemc_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return CEMC_ERR_ARG;
+  snprintf(buf, len, "%s", g_err.c_str());
+  return CEMC_OK;
+}
+
+extern "C" int cemc_version(int32_t *major, int32_t *minor, int32_t *sm) {
+  if (major) *major = 1;
+  if (minor) *minor = 0;
+  if (sm) *sm = 103;
+  return CEMC_OK;
+}
+
+extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry **out) {
+  if (!d || !out) return fail(CEMC_ERR_ARG, "null descriptor or output");
+  *out = nullptr;
+  const int N = d->n_sites, C = d->n_cols, S = d->n_sym, B = d->n_bf, K = d->n_eci, T = d->n_terms;
+  if (N <= 0 || C <= 0 || K <= 0 || T < 0) return fail(CEMC_ERR_ARG, "empty geometry");
+  if (C > CEMC_MAX_COLS) return fail(CEMC_ERR_LIMIT, "%d neighbour columns exceed the limit %d", C, CEMC_MAX_COLS);
+  if (B < 1 || B > CEMC_MAX_BF || S != B + 1 || S > 8)
+    return fail(CEMC_ERR_LIMIT, "unsupported species count %d", S);
+  if (K > CEMC_MAX_ECI) return fail(CEMC_ERR_LIMIT, "%d ECIs exceed the limit %d", K, CEMC_MAX_ECI);
+  if (!d->table || !d->bf || !d->eci_kind || !d->eci_dec || !d->eci_weight || !d->eci_full_weight ||
+      (T > 0 && (!d->term_eci || !d->term_ref || !d->term_size || !d->term_nb)))
+    return fail(CEMC_ERR_ARG, "null table pointer");
+  const int one_idx = C * B;
+  if (one_idx + 1 + B >= (1 << cemc::kRefBits)) return fail(CEMC_ERR_LIMIT, "neighbour table too wide");
+  for (size_t i = 0; i < (size_t)N * C; ++i)
+    if (d->table[i] < 0 || d->table[i] >= N) return fail(CEMC_ERR_ARG, "table entry %zu out of range", i);
+  int singlet[CEMC_MAX_BF];
+  for (int b = 0; b < CEMC_MAX_BF; ++b) singlet[b] = 0;
+  for (int k = 0; k < K; ++k) {
+    if (d->eci_kind[k] < 0 || d->eci_kind[k] > 2) return fail(CEMC_ERR_ARG, "bad ECI kind");
+    if (d->eci_kind[k] == 1) {
+      if (d->eci_dec[k] < 0 || d->eci_dec[k] >= B) return fail(CEMC_ERR_ARG, "bad singlet decoration");
+      singlet[d->eci_dec[k]] = k;
+    }
+  }
+  for (int t = 0; t < T; ++t) {
+    const int k = d->term_eci[t];
+    if (k < 0 || k >= K || d->eci_kind[k] != 2) return fail(CEMC_ERR_ARG, "term %d has a bad ECI", t);
+    if (t > 0 && k < d->term_eci[t - 1]) return fail(CEMC_ERR_ARG, "terms are not sorted by ECI");
+    if (d->term_size[t] < 2 || d->term_size[t] > 4) return fail(CEMC_ERR_ARG, "term %d has a bad size", t);
+    if (d->term_ref[t] < 0 || d->term_ref[t] >= B) return fail(CEMC_ERR_ARG, "term %d has a bad decoration", t);
+    for (int j = 0; j < d->term_size[t] - 1; ++j)
+      if (d->term_nb[3 * t + j] < 0 || d->term_nb[3 * t + j] >= one_idx)
+        return fail(CEMC_ERR_ARG, "term %d has a bad member", t);
+  }
+
+  // Lane chunks.
+  std::vector<int32_t> lane_term(33), first(32, 0), eci_lane(2 * (size_t)K);
+  for (int l = 0; l <= 32; ++l) lane_term[l] = (int32_t)(((long long)l * T) / 32);
+  int n_slots = 1;
+  for (int k = 0; k < K; ++k) {
+    eci_lane[2 * k] = 0;
+    eci_lane[2 * k + 1] = -1;
+  }
+  std::vector<int> lo_seen(K, 33), hi_seen(K, -1);
+  for (int l = 0; l < 32; ++l) {
+    const int lo = lane_term[l], hi = lane_term[l + 1];
+    if (lo >= hi) continue;
+    first[l] = d->term_eci[lo];
+    n_slots = std::max(n_slots, d->term_eci[hi - 1] - first[l] + 1);
+    for (int i = lo; i < hi; ++i) {
+      const int k = d->term_eci[i];
+      lo_seen[k] = std::min(lo_seen[k], l);
+      hi_seen[k] = std::max(hi_seen[k], l);
+    }
+  }
+  if (n_slots > cemc::kMaxSlots) return fail(CEMC_ERR_LIMIT, "a lane chunk spans %d ECIs", n_slots);
+  for (int k = 0; k < K; ++k)
+    if (hi_seen[k] >= 0) {
+      eci_lane[2 * k] = lo_seen[k];
+      eci_lane[2 * k + 1] = hi_seen[k];
+    }
+  std::vector<uint16_t> terms(4 * (size_t)std::max(T, 1), 0);
+  std::vector<uint8_t> fterms(8 * (size_t)std::max(T, 1), 0);
+  for (int l = 0; l < 32; ++l)
+    for (int i = lane_term[l]; i < lane_term[l + 1]; ++i) {
+      const int slot = d->term_eci[i] - first[l];
+      terms[4 * i] = (uint16_t)((one_idx + 1 + d->term_ref[i]) | (slot << cemc::kRefBits));
+      for (int j = 0; j < 3; ++j)
+        terms[4 * i + 1 + j] = (uint16_t)(j < d->term_size[i] - 1 ? d->term_nb[3 * i + j] : one_idx);
+    }
+  for (int i = 0; i < T; ++i) {
+    for (int j = 0; j < 3; ++j) {
+      const bool has = j < d->term_size[i] - 1;
+      fterms[8 * i + j] = (uint8_t)(has ? d->term_nb[3 * i + j] / B : 0);
+      fterms[8 * i + 3 + j] = (uint8_t)(has ? d->term_nb[3 * i + j] % B : 0);
+    }
+    fterms[8 * i + 6] = (uint8_t)d->term_ref[i];
+    fterms[8 * i + 7] = (uint8_t)d->term_size[i];
+  }
+  std::vector<int32_t> fterm_off(K + 1, 0);
+  {
+    int t = 0;
+    for (int k = 0; k < K; ++k) {
+      fterm_off[k] = t;
+      while (t < T && d->term_eci[t] == k) ++t;
+    }
+    fterm_off[K] = T;
+  }
+  // The trial kernel's conflict test needs a symmetric neighbour relation:
+  // j in row(i) <=> i in row(j).
+  {
+    std::vector<int32_t> sorted_rows(d->table, d->table + (size_t)N * C);
+    for (int i = 0; i < N; ++i) std::sort(sorted_rows.begin() + (size_t)i * C, sorted_rows.begin() + (size_t)(i + 1) * C);
+    for (int i = 0; i < N; ++i)
+      for (int c = 0; c < C; ++c) {
+        const int j = d->table[(size_t)i * C + c];
+        auto b = sorted_rows.begin() + (size_t)j * C, e = b + C;
+        if (!std::binary_search(b, e, i))
+          return fail(CEMC_ERR_ARG, "neighbour relation is not symmetric (site %d in row %d but not back)", j, i);
+      }
+  }
+  const int cpad = (C + 3) & ~3;
+  std::vector<int32_t> table_pad((size_t)N * cpad);
+  for (int i = 0; i < N; ++i)
+    for (int c = 0; c < cpad; ++c) table_pad[(size_t)i * cpad + c] = d->table[(size_t)i * C + (c < C ? c : 0)];
+  std::vector<int32_t> table_cm((size_t)N * C);
+  for (int i = 0; i < N; ++i)
+    for (int c = 0; c < C; ++c) table_cm[(size_t)c * N + i] = d->table[(size_t)i * C + c];
+  std::vector<double> w(d->eci_weight, d->eci_weight + K), fw(d->eci_full_weight, d->eci_full_weight + K);
+
+  // One device allocation for all tables.
+  struct Part {
+    const void *src;
+    size_t bytes;
+    size_t off;
+  };
+  std::vector<Part> parts = {
+      {table_pad.data(), sizeof(int32_t) * N * cpad, 0}, {table_cm.data(), sizeof(int32_t) * N * C, 0},
+      {terms.data(), terms.size() * 2, 0},         {lane_term.data(), 33 * 4, 0},
+      {first.data(), 32 * 4, 0},                   {eci_lane.data(), eci_lane.size() * 4, 0},
+      {d->eci_kind, sizeof(int32_t) * K, 0},       {d->eci_dec, sizeof(int32_t) * K, 0},
+      {w.data(), sizeof(double) * K, 0},           {fw.data(), sizeof(double) * K, 0},
+      {d->bf, sizeof(double) * B * S, 0},          {fterms.data(), fterms.size(), 0},
+      {fterm_off.data(), fterm_off.size() * 4, 0},
+  };
+  size_t total = 0;
+  for (auto &p : parts) {
+    p.off = total;
+    total = align_up(total + p.bytes, 256);
+  }
+  cemc_geometry *geo = new cemc_geometry();
+  cudaError_t e = cudaMalloc(&geo->dev, total);
+  if (e != cudaSuccess) {
+    delete geo;
+    return cuda_fail(e, "cudaMalloc(geometry tables)");
+  }
+  std::vector<unsigned char> host(total, 0);
+  for (auto &p : parts) memcpy(host.data() + p.off, p.src, p.bytes);
+  e = cudaMemcpy(geo->dev, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(geo->dev);
+    delete geo;
+    return cuda_fail(e, "cudaMemcpy(geometry tables)");
+  }
+  unsigned char *base = static_cast<unsigned char *>(geo->dev);
+  cemc::DevGeo &g = geo->g;
+  g.n_sites = N;
+  g.n_cols = C;
+  g.n_sym = S;
+  g.n_bf = B;
+  g.n_eci = K;
+  g.n_terms = T;
+  g.vals_len = one_idx + 1 + B;
+  g.one_idx = one_idx;
+  g.n_slots = n_slots;
+  g.cpad = cpad;
+  g.table = reinterpret_cast<const int32_t *>(base + parts[0].off);
+  g.table_cm = reinterpret_cast<const int32_t *>(base + parts[1].off);
+  g.terms = reinterpret_cast<const uint16_t *>(base + parts[2].off);
+  g.lane_term = reinterpret_cast<const int32_t *>(base + parts[3].off);
+  g.lane_first_eci = reinterpret_cast<const int32_t *>(base + parts[4].off);
+  g.eci_lane = reinterpret_cast<const int32_t *>(base + parts[5].off);
+  g.eci_kind = reinterpret_cast<const int32_t *>(base + parts[6].off);
+  g.eci_dec = reinterpret_cast<const int32_t *>(base + parts[7].off);
+  g.eci_w = reinterpret_cast<const double *>(base + parts[8].off);
+  g.eci_fw = reinterpret_cast<const double *>(base + parts[9].off);
+  g.bf = reinterpret_cast<const double *>(base + parts[10].off);
+  g.fterms = reinterpret_cast<const uint8_t *>(base + parts[11].off);
+  g.fterm_off = reinterpret_cast<const int32_t *>(base + parts[12].off);
+  for (int b = 0; b < CEMC_MAX_BF; ++b) g.singlet_eci[b] = singlet[b];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&geo->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  *out = geo;
+  return CEMC_OK;
+}
+
+extern "C" int cemc_geometry_destroy(cemc_geometry *geo) {
+  if (!geo) return CEMC_OK;
+  cudaError_t e = cudaFree(geo->dev);
+  delete geo;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaFree(geometry tables)");
+  return CEMC_OK;
+}
+
+extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *stream) {
+  if (!geo || !r) return fail(CEMC_ERR_ARG, "null geometry or run descriptor");
+  const cemc::DevGeo &g = geo->g;
+  if (r->n_chains <= 0) return fail(CEMC_ERR_ARG, "no chains");
+  if (r->move != CEMC_MOVE_FLIP && r->move != CEMC_MOVE_SWAP) return fail(CEMC_ERR_ARG, "unknown move type");
+  if (r->precision != CEMC_PREC_F32 && r->precision != CEMC_PREC_F64) return fail(CEMC_ERR_ARG, "unknown precision");
+  if (!r->occ || !r->cf || !r->energy || !r->eci || !r->kT || !r->trial)
+    return fail(CEMC_ERR_ARG, "null chain state pointer");
+  if (r->move == CEMC_MOVE_SWAP && (!r->trk || !r->loc || !r->trk_start || !r->trk_count))
+    return fail(CEMC_ERR_ARG, "swap moves need the per-species site lists");
+  if ((r->trace_site || r->trace_acc || r->trace_de) && !(r->trace_site && r->trace_acc && r->trace_de))
+    return fail(CEMC_ERR_ARG, "trace buffers must be given together");
+  if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
+  if (r->n_trials == 0) return CEMC_OK;
+  int warps = r->warps > 0 ? r->warps : 16;
+  if (warps > cemc::kMaxEval) warps = cemc::kMaxEval;
+  const int rsize = r->precision == CEMC_PREC_F32 ? 4 : 8;
+  cemc::RunArgs a;
+  a.n_chains = r->n_chains;
+  a.warps = warps;
+  a.seed = r->seed;
+  a.occ = r->occ;
+  a.cf = r->cf;
+  a.energy = r->energy;
+  a.eci = r->eci;
+  a.kT = r->kT;
+  a.trial = r->trial;
+  a.accum = r->accum;
+  a.trk = r->trk;
+  a.loc = r->loc;
+  a.trk_start = r->trk_start;
+  a.trk_count = r->trk_count;
+  a.trace_site = r->trace_site;
+  a.trace_acc = r->trace_acc;
+  a.trace_de = r->trace_de;
+  a.status = r->status;
+  a.chain_key = r->chain_key;
+  // Shared memory: the occupation, then (swaps) the site lists, then an exact
+  // stamp table (one entry per site) are preferred; fall back in that order.
+  const size_t budget = (size_t)geo->max_smem;
+  int exact_bits = 0;
+  while ((1 << exact_bits) < g.n_sites) ++exact_bits;
+  if (exact_bits < 5) exact_bits = 5;
+  const int is_swap = r->move == CEMC_MOVE_SWAP;
+  struct Choice {
+    int occ, trk, min_bits;
+  };
+  const Choice choices[] = {{1, is_swap, exact_bits}, {1, 0, exact_bits}, {1, 0, 12}, {0, 0, 12}, {0, 0, 5}};
+  bool found = false;
+  cemc::McLayout L{};
+  for (const Choice &ch : choices) {
+    for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
+      L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits);
+      if (L.total <= budget) {
+        a.occ_smem = ch.occ;
+        a.trk_smem = ch.trk;
+        a.stamp_bits = bits;
+        found = true;
+        break;
+      }
+    }
+    if (found) break;
+  }
+  if (!found) return fail(CEMC_ERR_LIMIT, "shared memory exceeds %zu bytes; use fewer warps", budget);
+  // Rounds are numbered in 27 bits of the stamp marks: split very long runs.
+  const uint64_t max_chunk = (uint64_t)1 << 26;
+  if (r->n_trials > max_chunk && r->trace_acc)
+    return fail(CEMC_ERR_LIMIT, "traced runs are limited to %llu trials per call", (unsigned long long)max_chunk);
+  for (uint64_t done = 0; done < r->n_trials;) {
+    const uint64_t n = std::min(max_chunk, r->n_trials - done);
+    a.n_trials = n;
+    cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "Monte Carlo kernel launch");
+    done += n;
+  }
+  return CEMC_OK;
+}
+
+extern "C" size_t cemc_recompute_scratch_doubles(const cemc_geometry *geo, int32_t n_chains) {
+  if (!geo || n_chains <= 0) return 0;
+  return cemc::recompute_blocks(geo->g) * (size_t)n_chains * (size_t)geo->g.n_eci;
+}
+
+extern "C" int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
+                              double *cf, double *energy, double *scratch, void *stream) {
+  if (!geo || n_chains <= 0 || !occ || !eci || !cf || !energy || !scratch)
+    return fail(CEMC_ERR_ARG, "bad recompute arguments");
+  if (n_chains > 65535) return fail(CEMC_ERR_LIMIT, "too many chains in one recompute");
+  cudaError_t e = cemc::launch_recompute(geo->g, n_chains, occ, eci, cf, energy, scratch,
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "recompute kernel launch");
+  return CEMC_OK;
+}
+
+extern "C" int cemc_energy(const cemc_geometry *geo, int32_t n_chains, const double *eci, const double *cf,
+                           double *energy, void *stream) {
+  if (!geo || n_chains <= 0 || !eci || !cf || !energy) return fail(CEMC_ERR_ARG, "bad energy arguments");
+  cudaError_t e = cemc::launch_energy(geo->g, n_chains, eci, cf, energy, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "energy kernel launch");
+  return CEMC_OK;
+}
+
+extern "C" int cemc_apply_changes(const cemc_geometry *geo, int8_t *occ, double *cf, double *energy,
+                                  const double *eci, int32_t n_changes, const int32_t *sites, const int8_t *old_sym,
+                                  const int8_t *new_sym, int32_t *status, void *stream) {
+  if (!geo || !occ || !cf || !energy || !eci || n_changes < 0 || (n_changes > 0 && (!sites || !old_sym || !new_sym)))
+    return fail(CEMC_ERR_ARG, "bad apply_changes arguments");
+  if (cemc::warp_kernel_smem(geo->g) > (size_t)geo->max_smem) return fail(CEMC_ERR_LIMIT, "tables too large");
+  cudaError_t e = cemc::launch_apply(geo->g, occ, cf, energy, eci, n_changes, sites, old_sym, new_sym, status,
+                                     static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "apply_changes kernel launch");
+  return CEMC_OK;
+}
+
+extern "C" int cemc_delta_e(const cemc_geometry *geo, const int8_t *occ, const double *eci, int32_t move,
+                            int32_t site_a, int32_t site_b, int32_t new_a, double *de_out, double *dcf_out,
+                            void *stream) {
+  if (!geo || !occ || !eci || !de_out || !dcf_out) return fail(CEMC_ERR_ARG, "bad delta_e arguments");
+  const cemc::DevGeo &g = geo->g;
+  if (site_a < 0 || site_a >= g.n_sites) return fail(CEMC_ERR_ARG, "site out of range");
+  if (move == CEMC_MOVE_SWAP && (site_b < 0 || site_b >= g.n_sites || site_b == site_a))
+    return fail(CEMC_ERR_ARG, "bad swap partner");
+  if (move == CEMC_MOVE_FLIP && (new_a < 0 || new_a >= g.n_sym)) return fail(CEMC_ERR_ARG, "bad species");
+  cudaError_t e = cemc::launch_delta(g, occ, eci, move, site_a, site_b, new_a, de_out, dcf_out,
+                                     static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "delta_e kernel launch");
+  return CEMC_OK;
+}
+
+extern "C" int cemc_pt_exchange(int32_t n_replicas, int32_t direction, uint64_t seed, uint64_t round,
+                                const double *energy, double *kT, int32_t *replica_of, int32_t *n_accept,
+                                void *stream) {
+  if (n_replicas < 1 || !energy || !kT || !replica_of || (direction != 0 && direction != 1))
+    return fail(CEMC_ERR_ARG, "bad replica-exchange arguments");
+  cudaError_t e = cemc::launch_pt(n_replicas, direction, seed, round, energy, kT, replica_of, n_accept,
+                                  static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "replica-exchange kernel launch");
+  return CEMC_OK;
+}

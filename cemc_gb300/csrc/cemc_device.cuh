@@ -1,0 +1,163 @@
+// Device-side data layout and building blocks shared by the CE Monte Carlo kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/cemc_gb300.h"
+#include "philox.h"
+
+namespace cemc {
+
+constexpr int kWarp = 32;
+constexpr int kMaxWarps = 32;
+constexpr int kMaxSlots = 31;      // ECIs one lane's chunk of terms may touch (5-bit field)
+constexpr int kRefBits = 11;       // low bits of a term's first field: vals index of the delta
+constexpr unsigned kFull = 0xffffffffu;
+
+// Device copy of one geometry (supercell + cluster expansion).
+//
+// Trial-move terms: the flattened (cluster ECI, equivalent decoration,
+// sub-cluster) products of a site, sorted by ECI and cut into 32 contiguous
+// chunks, one per lane.  Each term is 4 x uint16:
+//   f[0] = (vals index of delta[d_ref]) | (slot << 11)
+//   f[1..3] = vals index of (column, decoration) of members 1..3, or the
+//             index of the constant 1.0 for absent members.
+// "vals" is a per-warp array: bf[d][species of neighbour c] at c * n_bf + d,
+// 1.0 at n_cols * n_bf, delta[d] = bf[d][new] - bf[d][old] right after.
+// The slot is the ECI index relative to the first ECI of the lane's chunk.
+struct DevGeo {
+  int n_sites, n_cols, n_sym, n_bf, n_eci, n_terms;
+  int vals_len;    // n_cols * n_bf + 1 + n_bf
+  int one_idx;     // n_cols * n_bf
+  int n_slots;     // max ECIs per lane chunk
+  int cpad;        // row stride of `table`: n_cols rounded up to a multiple of 4 (16-byte rows)
+  const int32_t *table;     // [n_sites * cpad] row-major (trial moves), padding columns repeat column 0
+  const int32_t *table_cm;  // [n_cols * n_sites] column-major (full recompute)
+  const uint16_t *terms;    // [n_terms * 4]
+  const int32_t *lane_term; // [33] chunk boundaries
+  const int32_t *lane_first_eci;  // [32]
+  const int32_t *eci_lane;  // [n_eci * 2] first and last lane holding terms of the ECI (last < first: none)
+  const int32_t *eci_kind;  // [n_eci]
+  const int32_t *eci_dec;   // [n_eci]
+  const double *eci_w;      // [n_eci] increment weight (cluster), 0 otherwise
+  const double *eci_fw;     // [n_eci] full-recompute weight (cluster)
+  const double *bf;         // [n_bf * n_sym]
+  const uint8_t *fterms;    // [n_terms * 8] {col0, col1, col2, d0, d1, d2, d_ref, size}
+  const int32_t *fterm_off; // [n_eci + 1] ranges of fterms per ECI
+  int singlet_eci[CEMC_MAX_BF];
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+template <typename R>
+__device__ __forceinline__ R warp_scan_incl(R v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const R n = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += n;
+  }
+  return v;
+}
+
+// Metropolis test of the reference, accept = (dE < 0) or (u <= exp(-dE / kT))
+// (cemc/mcmc/montecarlo.py:950-956).  The comparison is first made as
+// ln(u) + dE/kT against a margin in single precision on the special-function
+// unit; only trials within the margin of the threshold evaluate the exact
+// double-precision form, so the decision equals the double-precision one.
+__device__ __forceinline__ int metropolis(double de, double u, double kT, float inv_kT) {
+  if (de < 0.0) return 1;
+  const float x = (float)de * inv_kT;
+  const float y = __logf((float)u) + x;
+  const float margin = 1e-4f + 1e-6f * x;
+  if (y < -margin) return 1;
+  if (y > margin) return 0;
+  return u <= exp(-de / kT);
+}
+
+// Fill one warp's vals array for a change of `site` from species `old_s` to
+// `new_s`.  Neighbour species come from `occ`, except that `ovr_site` (if >=
+// 0) is read as species `ovr_s` (the first half of a swap already applied).
+// Each lane keeps the neighbour site ids of its columns in nbr[] for the
+// conflict test.
+template <typename R>
+__device__ __forceinline__ void gather_vals(const DevGeo &g, const int8_t *occ, const R *bf_s, int site, int old_s,
+                                            int new_s, int ovr_site, int ovr_s, R *vals, int (&nbr)[4], int lane) {
+  const int32_t *row = g.table + (size_t)site * g.cpad;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = lane + 32 * j;
+    nbr[j] = -1;
+    if (c < g.n_cols) {
+      const int s = __ldg(row + c);
+      nbr[j] = s;
+      const int o = (s == ovr_site) ? ovr_s : (int)occ[s];
+      for (int d = 0; d < g.n_bf; ++d) vals[c * g.n_bf + d] = bf_s[d * g.n_sym + o];
+    }
+  }
+  if (lane == 0) {
+    vals[g.one_idx] = (R)1;
+    for (int d = 0; d < g.n_bf; ++d) vals[g.one_idx + 1 + d] = bf_s[d * g.n_sym + new_s] - bf_s[d * g.n_sym + old_s];
+  }
+}
+
+// Sum this lane's chunk of terms into per-slot partials part[slot * 32 + lane].
+// With TWO, the product over a second vals array (the second site of a swap)
+// is added term by term.
+template <typename R, bool TWO>
+__device__ __forceinline__ void lane_terms(const DevGeo &g, const uint16_t *terms_s, const int32_t *lane_term_s,
+                                           const R *va, const R *vb, R *part, int lane) {
+  for (int s = 0; s < g.n_slots; ++s) part[s * 32 + lane] = (R)0;
+  const int lo = lane_term_s[lane], hi = lane_term_s[lane + 1];
+  if (lo >= hi) return;
+  int cur = terms_s[4 * lo] >> kRefBits;
+  R acc = (R)0;
+  for (int i = lo; i < hi; ++i) {
+    const uint2 packed = *reinterpret_cast<const uint2 *>(terms_s + 4 * i);
+    const int f0 = packed.x & 0xffff, f1 = packed.x >> 16, f2 = packed.y & 0xffff, f3 = packed.y >> 16;
+    const int sl = f0 >> kRefBits, ri = f0 & ((1 << kRefBits) - 1);
+    if (sl != cur) {
+      part[cur * 32 + lane] = acc;
+      acc = (R)0;
+      cur = sl;
+    }
+    R p = va[ri] * va[f1] * va[f2] * va[f3];
+    if (TWO) p += vb[ri] * vb[f1] * vb[f2] * vb[f3];
+    acc += p;
+  }
+  part[cur * 32 + lane] = acc;
+}
+
+// Combine per-lane partials into the per-ECI change D[k] (unweighted term sum
+// for cluster ECIs, delta[d] for singlets) and return the energy change
+// sum_k coef[k] * D[k] (coef = N * eci * weight), identical on all lanes.
+template <typename R, bool TWO>
+__device__ __forceinline__ R eci_changes(const DevGeo &g, const int32_t *eci_lane_s, const int32_t *first_s,
+                                         const int8_t *kind_s, const int8_t *dec_s, const R *coef_s, const R *part,
+                                         const R *va, const R *vb, R *D, int lane) {
+  R de = (R)0;
+  for (int k = lane; k < g.n_eci; k += 32) {
+    R v = (R)0;
+    const int kind = kind_s[k];
+    if (kind == 2) {
+      const int lo = eci_lane_s[2 * k], hi = eci_lane_s[2 * k + 1];
+      for (int l = lo; l <= hi; ++l) v += part[(k - first_s[l]) * 32 + l];
+    } else if (kind == 1) {
+      const int d = dec_s[k];
+      v = va[g.one_idx + 1 + d];
+      if (TWO) v += vb[g.one_idx + 1 + d];
+    }
+    D[k] = v;
+    de += coef_s[k] * v;
+  }
+  return warp_sum(de);
+}
+
+}  // namespace cemc

@@ -1,0 +1,110 @@
+// Launch arguments and the shared-memory layout of the Monte Carlo kernel,
+// computed identically on the host (to size the launch) and on the device.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cemc_device.cuh"
+
+namespace cemc {
+
+struct RunArgs {
+  int n_chains, warps;
+  int occ_smem, trk_smem;  // 1: the chain's occupation / swap tracker lives in shared memory
+  int stamp_bits;          // log2 of the conflict-stamp table size
+  uint64_t seed, n_trials;
+  int8_t *occ;
+  double *cf, *energy;
+  const double *eci, *kT;
+  uint64_t *trial;
+  cemc_accum *accum;
+  int32_t *trk, *loc;
+  const int32_t *trk_start, *trk_count;
+  int32_t *trace_site;
+  int8_t *trace_acc;
+  double *trace_de;
+  int32_t *status;
+  const uint32_t *chain_key;
+};
+
+constexpr int kRing = 128;     // trial slots of the draw / row ring (power of two, > 3 * kMaxEval)
+constexpr int kMaxEval = 31;   // trial-evaluating warps; one more warp is the helper
+
+// Per-trial draw, written by the helper warp: site (flips), Philox words.
+struct Draw {
+  int32_t site;
+  uint32_t w1, w2, w3, w0, x0, x1, pad;
+};
+
+struct McLayout {
+  size_t cf, eci, w, acc, coef, bf, terms, lane_term, kind, misc;
+  size_t rec, rec_stride, rec_tsa, rec_tsb, rec_acc, rec_der, rec_de, rec_d;
+  size_t draws, rows;
+  size_t warp0, warp_stride, warp_part;
+  size_t occ, trk, stamp;
+  int stamp_bits;
+  size_t total;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Shared-memory carve-up of mc_kernel for `warps` evaluating warps.
+__host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
+                                              int trk_smem, int stamp_bits) {
+  McLayout L;
+  size_t o = 0;
+  const size_t K = (size_t)g.n_eci;
+  L.cf = o;
+  o = align16(o + 8 * K);
+  L.eci = o;
+  o = align16(o + 8 * K);
+  L.w = o;
+  o = align16(o + 8 * K);
+  L.acc = o;
+  o = align16(o + 8 * (size_t)(2 + 3 * CEMC_MAX_BF));
+  L.coef = o;
+  o = align16(o + (size_t)rsize * K);
+  L.bf = o;
+  o = align16(o + (size_t)rsize * g.n_bf * g.n_sym);
+  L.terms = o;
+  o = align16(o + 8 * (size_t)g.n_terms);
+  L.lane_term = o;
+  o = align16(o + 4 * (size_t)(33 + 32 + 2 * K));
+  L.kind = o;
+  o = align16(o + 2 * K);
+  L.misc = o;
+  o = align16(o + 4 * 64);
+  // two buffers of per-trial records (current round / round being booked)
+  L.rec_tsa = 0;
+  L.rec_tsb = 4 * 32;
+  L.rec_acc = 8 * 32;
+  L.rec_der = align16(L.rec_acc + 32);
+  L.rec_de = align16(L.rec_der + (size_t)rsize * 32);
+  L.rec_d = align16(L.rec_de + 8 * 32);
+  L.rec_stride = align16(L.rec_d + (size_t)rsize * 32 * K);
+  L.rec = o;
+  o = align16(o + 2 * L.rec_stride);
+  L.draws = o;
+  o = align16(o + sizeof(Draw) * (size_t)kRing);
+  L.rows = o;
+  if (move == CEMC_MOVE_FLIP) o = align16(o + 4 * (size_t)kRing * g.cpad);
+  const size_t vals = (size_t)rsize * g.vals_len * (move == CEMC_MOVE_SWAP ? 2 : 1);
+  L.warp_part = align16(vals);
+  L.warp_stride = align16(L.warp_part + (size_t)rsize * g.n_slots * 32);
+  L.warp0 = o;
+  o = align16(o + L.warp_stride * (size_t)warps);
+  L.stamp_bits = stamp_bits;
+  L.stamp = o;
+  o = align16(o + 4 * ((size_t)1 << stamp_bits));
+  L.occ = o;
+  if (occ_smem) o = align16(o + (size_t)g.n_sites);
+  L.trk = o;
+  if (trk_smem) o = align16(o + 8 * (size_t)g.n_sites);
+  L.total = o;
+  return L;
+}
+
+cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st);
+
+}  // namespace cemc

@@ -127,6 +127,7 @@ typedef struct {
   int8_t *trace_acc;
   double *trace_de;
   int32_t *status;     /* [n_chains] device status words, may be NULL */
+  const uint32_t *chain_key; /* [n_chains] RNG key of each chain (device), NULL = chain index */
 } cemc_run_desc;
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
@@ -144,6 +145,12 @@ int cemc_run(const cemc_geometry *geo, const cemc_run_desc *run, void *stream);
 size_t cemc_recompute_scratch_doubles(const cemc_geometry *geo, int32_t n_chains);
 int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
                    double *cf, double *energy, double *scratch, void *stream);
+
+/* Energy N * sum_k eci[k] * cf[k] of every chain, summed in sorted-name order
+ * (CEUpdater::get_energy + NamedArray::dot, ce_updater.cpp:236-242,
+ * named_array.cpp:25-33).  Device pointers. */
+int cemc_energy(const cemc_geometry *geo, int32_t n_chains, const double *eci, const double *cf, double *energy,
+                void *stream);
 
 /* Apply an explicit list of single-site changes in sequence to one chain
  * (CEUpdater::calculate / update_cf, ce_updater.cpp:313-406, 471-519, 845-853):

@@ -245,14 +245,23 @@ class _Atom:
         self.index = index
 
 
+_KEEP_ALIVE: List[object] = []
+
+
 def make_reference_updater(settings, symbols: Sequence[str], cf: Dict[str, float], eci: Dict[str, float]):
-    """A reference ``PyCEUpdater`` over a plain list of atoms; returns (updater, atoms)."""
+    """A reference ``PyCEUpdater`` over a plain list of atoms; returns (updater, atoms).
+
+    ``CEUpdater`` stores the atoms object without taking a reference and
+    releases one in its destructor (cpp/src/ce_updater.cpp:22, 33).  The
+    harness therefore takes that reference on its behalf and keeps the list
+    alive for the life of the process.
+    """
+    import ctypes
     mod = reference_module()
     if mod is None:
         raise RuntimeError("reference CEUpdater not built (oracle/build_ref.sh)")
     atoms = [_Atom(s, i) for i, s in enumerate(symbols)]
-    import contextlib
-    import io
-    with contextlib.redirect_stdout(io.StringIO()):
-        upd = mod.PyCEUpdater(atoms, settings, dict(cf), dict(eci))
+    ctypes.pythonapi.Py_IncRef(ctypes.py_object(atoms))
+    _KEEP_ALIVE.append(atoms)
+    upd = mod.PyCEUpdater(atoms, settings, dict(cf), dict(eci))
     return upd, atoms

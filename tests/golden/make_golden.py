@@ -1,0 +1,148 @@
+"""Generate the golden fixtures of the hot path from the reference's own CEUpdater.
+
+Run in a checkout where the reference has been compiled by
+``oracle/build_ref.sh`` (it needs the reference sources).  For each case it
+
+1. builds an FCC supercell and cluster set with ``cemc_gb300.lattice``;
+2. draws a random occupation and computes its correlation functions with the
+   oracle's full recompute (the reference has no full recompute of its own;
+   its tests compare against CLEASE's, which is unavailable);
+3. lets the oracle propose ``n_trials`` moves and uniforms from the shared
+   counter-based stream (seed, chain 0), and replays exactly those moves and
+   uniforms through the reference's ``PyCEUpdater.calculate`` /
+   ``clear_history`` / ``undo_changes`` with the reference's Metropolis rule
+   (cemc/mcmc/montecarlo.py:950-956, 1014-1017);
+4. records the reference's decisions, energy changes, final occupation,
+   correlation functions and energy, plus the reference's correlation
+   functions after each of a few explicit single-site updates.
+
+The fixtures then pin the oracle (CPU tests) and the GPU path (GPU tests) to
+the reference on machines without the reference tree.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from cemc_gb300.lattice import fcc_settings, seeded_ecis  # noqa: E402
+from cemc_gb300.tables import CEModel  # noqa: E402
+
+KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
+
+# name, L, pair shells, triplet shells, quad shells, species, move (0 flip, 1 swap), T, trials, seed
+CASES = [
+    ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11),
+    ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12),
+    ("binary_swap_cold", 4, 4, 2, 1, ["Al", "Mg"], 1, 150.0, 3000, 13),
+    ("ternary_flip", 4, 5, 3, 1, ["Al", "Mg", "Si"], 0, 800.0, 1500, 14),
+    ("ternary_swap", 4, 5, 3, 1, ["Al", "Mg", "Si"], 1, 800.0, 1500, 15),
+]
+
+
+def model_hash(m: CEModel) -> str:
+    h = hashlib.sha256()
+    for a in (m.table, m.term_eci, m.term_ref, m.term_size, m.term_nb, m.eci_weight, m.bf):
+        h.update(np.ascontiguousarray(a).tobytes())
+    h.update("|".join(m.eci_names).encode())
+    return h.hexdigest()
+
+
+def build_case(name, L, ps, ts, qs, syms, move, T, n, seed):
+    import oracle as O
+    s = fcc_settings(L, ps, ts, qs, syms)
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    orc = O.Oracle(m)
+    rng = np.random.default_rng(seed)
+    occ0 = rng.integers(0, len(syms), m.n_sites).astype(np.int8)
+    ev = m.eci_vector(eci)
+    kT = KB * T
+    st = orc.new_chain_state(occ0, ev, kT, move)
+    cf0 = st.cf.copy()
+    tr = orc.run(st, seed=seed, chain_id=0, t_begin=0, n_trials=n, trace=True)
+
+    upd, _ = O.make_reference_updater(s, m.symbols_of(occ0), dict(zip(m.eci_names, cf0)), eci)
+    occ = occ0.copy()
+    cur = upd.get_energy()
+    acc = np.zeros(n, dtype=np.int8)
+    de = np.zeros(n)
+    for i in range(n):
+        a, b = int(tr.site[2 * i]), int(tr.site[2 * i + 1])
+        if move == 1:
+            A, B = occ[a], occ[b]
+            changes = [(a, m.symbols[A], m.symbols[B]), (b, m.symbols[B], m.symbols[A])]
+        else:
+            changes = [(a, m.symbols[occ[a]], m.symbols[b])]
+        new = upd.calculate(changes)
+        de[i] = new - cur
+        ok = True if new < cur else (tr.u[i] <= math.exp(-(new - cur) / kT))
+        acc[i] = ok
+        if ok:
+            upd.clear_history()
+            cur = new
+            for j, _, nw in changes:
+                occ[j] = m.symbols.index(nw)
+        else:
+            upd.undo_changes()
+    ref_cf = upd.get_cf()
+    cf_final = np.array([ref_cf[k] for k in m.eci_names])
+
+    # Known answers of explicit single-site updates (CEUpdater::update_cf).
+    upd2, _ = O.make_reference_updater(s, m.symbols_of(occ0), dict(zip(m.eci_names, cf0)), eci)
+    occ_u = occ0.copy()
+    n_upd = 12
+    upd_sites = rng.choice(m.n_sites, n_upd, replace=False).astype(np.int32)
+    upd_new = np.zeros(n_upd, dtype=np.int8)
+    upd_cf = np.zeros((n_upd, m.n_eci))
+    upd_e = np.zeros(n_upd)
+    for i, site in enumerate(upd_sites):
+        new = (occ_u[site] + 1 + rng.integers(len(syms) - 1)) % len(syms)
+        upd_new[i] = new
+        upd2.update_cf((int(site), m.symbols[occ_u[site]], m.symbols[new]))
+        occ_u[site] = new
+        c = upd2.get_cf()
+        upd_cf[i] = [c[k] for k in m.eci_names]
+        upd_e[i] = upd2.get_energy()
+
+    return dict(
+        L=L, shells=np.array([ps, ts, qs]), species=np.array(syms), move=move, T=T, kT=kT, seed=seed,
+        n_trials=n, model_hash=model_hash(m), eci=ev, eci_names=np.array(m.eci_names),
+        occ0=occ0, cf0=cf0, sites=tr.site.reshape(n, 2), u=tr.u, ref_acc=acc, ref_de=de,
+        occ_final=occ, cf_final=cf_final, energy_final=cur,
+        upd_sites=upd_sites, upd_new=upd_new, upd_cf=upd_cf, upd_energy=upd_e,
+    )
+
+
+def main():
+    import contextlib
+    out_dir = HERE
+    for case in CASES:
+        # the reference's init logs to the C++ streams; silence them at the fd level
+        with open(os.devnull, "w") as devnull, contextlib.ExitStack():
+            saved = os.dup(1), os.dup(2)
+            os.dup2(devnull.fileno(), 1)
+            os.dup2(devnull.fileno(), 2)
+            try:
+                data = build_case(*case)
+            finally:
+                os.dup2(saved[0], 1)
+                os.dup2(saved[1], 2)
+        path = os.path.join(out_dir, case[0] + ".npz")
+        np.savez_compressed(path, **data)
+        print("%s: %d trials, acceptance %.3f, final energy %.6f -> %s" % (
+            case[0], data["n_trials"], data["ref_acc"].mean(), data["energy_final"], os.path.basename(path)))
+
+
+if __name__ == "__main__":
+    main()

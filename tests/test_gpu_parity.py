@@ -1,0 +1,256 @@
+"""GPU kernels against the reference (golden fixtures) and the CPU oracle.
+
+Bar: bit-exact decisions and occupations; correlation functions and energies
+within 1e-9 relative in FP64; in FP32-energy-change mode, decisions bit-exact
+outside the near-threshold band |dE/kT + ln u| < FP32_BAND and energy-change
+error at most 1e-5 eV.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import KB, golden_cases, golden_model, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-9
+FP32_DE_TOL = 1e-5  # eV, per trial
+
+
+@pytest.fixture(scope="module")
+def E():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from cemc_gb300 import engine
+    return engine
+
+
+def _sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def _cf_close(a, b, rtol=FP64_RTOL, atol=1e-14):
+    return np.allclose(a, b, rtol=rtol, atol=atol)
+
+
+@pytest.mark.parametrize("warps", [1, 16, 32])
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_replays_reference_fixture_fp64(case, warps, E):
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    move = int(g["move"])
+    cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=int(g["seed"]))
+    assert _cf_close(cb.cf.cpu().numpy()[0], g["cf0"], atol=1e-15)
+    n = int(g["n_trials"])
+    sites, acc, de = cb.run(n, precision=E.PREC_F64, warps=warps, trace=True)
+    _sync()
+    cb.check_status()
+    assert np.array_equal(sites.cpu().numpy()[0], g["sites"])
+    assert np.array_equal(acc.cpu().numpy()[0], g["ref_acc"])
+    assert np.array_equal(cb.occ.cpu().numpy()[0], g["occ_final"])
+    assert _cf_close(cb.cf.cpu().numpy()[0], g["cf_final"])
+    assert _rel(cb.energy.cpu().numpy()[0], g["energy_final"]) < FP64_RTOL
+    assert np.max(np.abs(de.cpu().numpy()[0] - g["ref_de"])) < 1e-9
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_fp32_energy_change_against_reference_fixture(case, E):
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), int(g["move"]), seed=int(g["seed"]))
+    n = int(g["n_trials"])
+    sites, acc, de = cb.run(n, precision=E.PREC_F32, warps=16, trace=True)
+    _sync()
+    acc = acc.cpu().numpy()[0]
+    de = de.cpu().numpy()[0]
+    kT = float(g["kT"])
+    margin = np.abs(g["ref_de"] / kT + np.log(np.maximum(g["u"], 1e-300)))
+    band = FP32_DE_TOL / kT
+    near = margin < band
+    mism = acc != g["ref_acc"]
+    assert not np.any(mism & ~near), "decision differs outside the FP32 band"
+    if not np.any(mism):
+        assert np.array_equal(cb.occ.cpu().numpy()[0], g["occ_final"])
+        assert np.max(np.abs(de - g["ref_de"])) < FP32_DE_TOL
+        assert _cf_close(cb.cf.cpu().numpy()[0], g["cf_final"], rtol=1e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_calculator_kernels_match_reference_updates(case, E):
+    """cemc_apply_changes reproduces the reference's update_cf known answers."""
+    import torch
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    from cemc_gb300.calculator import DeviceUpdater
+    up = DeviceUpdater(geo, g["occ0"], g["eci"], cf=g["cf0"])
+    for i, site in enumerate(g["upd_sites"]):
+        up.apply([(int(site), int(up.occupation()[site]), int(g["upd_new"][i]))])
+        assert _cf_close(up.cf(), g["upd_cf"][i])
+        assert _rel(up.energy(), g["upd_energy"][i]) < FP64_RTOL
+
+
+def test_gpu_delta_e_matches_oracle(E, oracle_mod):
+    g = load_golden("ternary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    from cemc_gb300.calculator import DeviceUpdater
+    up = DeviceUpdater(geo, g["occ0"], g["eci"], cf=g["cf0"])
+    occ = g["occ0"].copy()
+    rng = np.random.default_rng(1)
+    e0 = orc.energy(g["eci"], g["cf0"])
+    for _ in range(20):
+        a, b = (int(x) for x in rng.choice(m.n_sites, 2, replace=False))
+        if occ[a] == occ[b]:
+            continue
+        de, dcf = up.delta_swap(a, b)
+        c1 = orc.update_cf(occ, a, occ[b], g["cf0"])
+        o2 = occ.copy()
+        o2[a] = occ[b]
+        c2 = orc.update_cf(o2, b, occ[a], c1)
+        assert abs(de - (orc.energy(g["eci"], c2) - e0)) < 1e-9
+        assert np.allclose(dcf, c2 - g["cf0"], atol=1e-13)
+
+
+@pytest.mark.parametrize("recipe", [(6, 4, 2, 1, ["Al", "Mg"]), (4, 5, 3, 1, ["Al", "Mg", "Si"])])
+def test_gpu_full_recompute_matches_oracle(recipe, E, oracle_mod):
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    L, ps, ts, qs, syms = recipe
+    s = fcc_settings(L, ps, ts, qs, syms)
+    eci = seeded_ecis(s.cset, 2)
+    m = CEModel(s, list(eci))
+    orc = oracle_mod.Oracle(m)
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(5)
+    occ = rng.integers(0, len(syms), (5, m.n_sites)).astype(np.int8)
+    cb = E.ChainBatch(geo, occ, m.eci_vector(eci), KB * 700, E.MOVE_FLIP)
+    _sync()
+    for c in range(5):
+        full = orc.full_cf(occ[c])
+        assert np.allclose(cb.cf.cpu().numpy()[c], full, rtol=1e-12, atol=1e-15)
+        assert _rel(cb.energy.cpu().numpy()[c], orc.energy(m.eci_vector(eci), full)) < 1e-12
+
+
+@pytest.mark.parametrize("move", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_batch_equals_oracle_per_chain(move, prec, E, oracle_mod):
+    """Many chains in one launch, each equal to the oracle run of that chain (keys, temperatures, mu differ)."""
+    g = load_golden("binary_flip")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(7)
+    n_chains = 6
+    occ = rng.integers(0, 2, (n_chains, m.n_sites)).astype(np.int8)
+    Ts = np.linspace(300, 1500, n_chains)
+    ev = np.repeat(g["eci"][None], n_chains, 0)
+    ev[:, m.eci_names.index("c1_0")] += np.linspace(-0.1, 0.1, n_chains)
+    keys = [11, 5, 7, 3, 13, 2]
+    cb = E.ChainBatch(geo, occ, ev, KB * Ts, move, seed=99, chain_keys=keys)
+    n = 2500
+    _, acc, de = cb.run(n, precision=prec, warps=8, trace=True)
+    _sync()
+    acc = acc.cpu().numpy()
+    de = de.cpu().numpy()
+    for c in range(n_chains):
+        st = orc.new_chain_state(occ[c], ev[c], KB * Ts[c], move)
+        tr = orc.run(st, seed=99, chain_id=keys[c], t_begin=0, n_trials=n, trace=True)
+        if prec == 0:
+            assert np.array_equal(acc[c], tr.acc)
+            assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
+            assert _cf_close(cb.cf.cpu().numpy()[c], st.cf)
+        else:
+            margin = np.abs(tr.de / (KB * Ts[c]) + np.log(np.maximum(tr.u, 1e-300)))
+            mism = acc[c] != tr.acc
+            assert not np.any(mism & (margin >= FP32_DE_TOL / (KB * Ts[c])))
+            if not np.any(mism):
+                assert np.max(np.abs(de[c] - tr.de)) < FP32_DE_TOL
+                assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
+
+
+def test_gpu_launch_splitting_is_invisible(E):
+    """k launches of n/k trials equal one launch of n (counter-based proposals, resident state)."""
+    g = load_golden("binary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    a = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
+    b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
+    a.run(3000, precision=0, warps=16)
+    for _ in range(3):
+        b.run(1000, precision=0, warps=7)
+    _sync()
+    assert np.array_equal(a.occ.cpu().numpy(), b.occ.cpu().numpy())
+    assert np.allclose(a.cf.cpu().numpy(), b.cf.cpu().numpy(), rtol=1e-12, atol=1e-15)
+    ha, hb = a.accum_host(), b.accum_host()
+    assert ha[0, E.A_NSAMP] == hb[0, E.A_NSAMP] == 3000
+    assert ha[0, E.A_NACC] == hb[0, E.A_NACC]
+
+
+def test_gpu_accumulators_match_oracle(E, oracle_mod):
+    g = load_golden("binary_flip")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    for prec in (0, 1):
+        cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 0, seed=int(g["seed"]))
+        cb.run(3000, precision=prec, warps=16)
+        _sync()
+        st = orc.new_chain_state(g["occ0"], g["eci"], float(g["kT"]), 0)
+        orc.run(st, seed=int(g["seed"]), chain_id=0, t_begin=0, n_trials=3000)
+        h = cb.accum_host()[0]
+        o = st.acc[0]
+        tol = 1e-9 if prec == 0 else 1e-5
+        assert h[E.A_NSAMP] == o["n_samples"] and h[E.A_NACC] == o["n_accept"]
+        n = o["n_samples"]
+        assert abs(h[E.A_SUM_E] - o["sum_e"]) / n < tol
+        assert abs(h[E.A_SUM_E2] - o["sum_e2"]) / n < tol * max(1.0, abs(o["sum_e2"] / n))
+        assert abs(h[E.A_SUM_S] - o["sum_s"][0]) / n < tol
+        assert abs(h[E.A_SUM_S2] - o["sum_s2"][0]) / n < tol
+        assert abs(h[E.A_SUM_SE] - o["sum_se"][0]) / n < tol
+
+
+def test_gpu_replica_exchange_matches_restatement(E):
+    """cemc_pt_exchange against a Python restatement of parallel_tempering.py:138-175."""
+    import torch
+    from cemc_gb300.rng import pt_uniform
+    n = 9
+    rng = np.random.default_rng(3)
+    energy = rng.normal(-100, 2, n)
+    Ts = np.geomspace(200, 1500, n)
+    for direction in (0, 1):
+        for rnd in range(4):
+            kT = KB * Ts.copy()
+            rep = np.arange(n, dtype=np.int32)
+            en_d = torch.tensor(energy, device="cuda")
+            kT_d = torch.tensor(kT, device="cuda")
+            rep_d = torch.tensor(rep, device="cuda")
+            nacc = torch.zeros(1, dtype=torch.int32, device="cuda")
+            from cemc_gb300.engine import pt_exchange
+            pt_exchange(en_d, kT_d, rep_d, direction, seed=17, round_index=rnd, n_accept=nacc)
+            _sync()
+            pairs = [(i, i + 1) for i in range(0, n - 1, 2)] if direction == 0 else \
+                    [(i, i - 1) for i in range(n - 1, 0, -2)]
+            acc = 0
+            for p, q in pairs:
+                ci, cj = rep[p], rep[q]
+                prob = math.exp((1 / kT[ci] - 1 / kT[cj]) * (energy[ci] - energy[cj]))
+                u = pt_uniform(17, rnd, p)
+                if u < prob:
+                    kT[ci], kT[cj] = kT[cj], kT[ci]
+                    rep[p], rep[q] = cj, ci
+                    acc += 1
+            assert np.array_equal(rep_d.cpu().numpy(), rep)
+            assert np.array_equal(kT_d.cpu().numpy(), kT)
+            assert int(nacc.item()) == acc

@@ -1,0 +1,151 @@
+"""Geometry and cluster generator: shells, cluster multiplicities, symmetry, names."""
+import itertools
+
+import numpy as np
+import pytest
+
+from cemc_gb300.lattice import (FCCSupercell, enumerate_cluster_types, equivalent_decorations, fcc_settings,
+                                fcc_shell_vectors, seeded_ecis)
+from cemc_gb300.tables import CEModel
+
+
+def test_fcc_shell_multiplicities():
+    shells = fcc_shell_vectors(6)
+    assert [len(s) for s in shells] == [12, 6, 24, 12, 24, 8]
+    assert [int((s[0] ** 2).sum()) for s in shells] == [2, 4, 6, 8, 10, 12]
+
+
+def test_supercell_indexing_roundtrip():
+    cell = FCCSupercell(3)
+    assert cell.n_sites == 4 * 27
+    idx = cell.index_of(cell.positions)
+    assert np.array_equal(idx, np.arange(cell.n_sites))
+    # periodic images map to the same site
+    assert np.array_equal(cell.index_of(cell.positions + 2 * cell.L), idx)
+
+
+def test_cluster_counts_binary_recipe():
+    types = enumerate_cluster_types(4, 2, 1)
+    got = [(t.size, t.dia2, len(t.offsets)) for t in types]
+    assert got == [(2, 2, 12), (2, 4, 6), (2, 6, 24), (2, 8, 12), (3, 2, 24), (3, 4, 36), (4, 2, 8)]
+    terms = sum(len(t.offsets) for t in types)
+    assert terms == 122  # sub-cluster products per flip of the binary recipe
+
+
+def test_cluster_orbits_cover_every_occurrence():
+    """Each cluster containing the origin appears once per (type, ordering) and every order maps onto the prototype."""
+    for t in enumerate_cluster_types(5, 3, 1):
+        seen = set()
+        for off, order in zip(t.offsets, t.order):
+            pts = np.vstack([np.zeros((1, 3), dtype=np.int64), off])
+            key = tuple(sorted(map(tuple, pts.tolist())))
+            assert key not in seen
+            seen.add(key)
+            # the canonical ordering reproduces the prototype's pairwise distances
+            ordered = pts[order]
+            d1 = ((ordered[:, None] - ordered[None]) ** 2).sum(-1)
+            p = t.prototype
+            d2 = ((p[:, None] - p[None]) ** 2).sum(-1)
+            assert np.array_equal(d1, d2)
+        # each cluster of size s is counted once per member: multiplicity divisible by size over the orbit
+        assert len(t.offsets) % 1 == 0
+
+
+@pytest.mark.parametrize("L", [4, 6])
+def test_neighbour_relation_is_symmetric(L):
+    s = fcc_settings(L, 4, 2, 1, ["Al", "Mg"])
+    tab = s.table
+    n = s.n_sites
+    for i in range(0, n, max(1, n // 37)):
+        for j in tab[i]:
+            assert i in set(tab[j].tolist())
+
+
+def test_no_self_interaction_and_distinct_members():
+    s = fcc_settings(4, 5, 3, 1, ["Al", "Mg", "Si"])
+    for name, info in s.cluster_info[0].items():
+        for sub in info["indices"]:
+            assert info["ref_indx"] not in sub
+            assert len(set(sub)) == len(sub)
+
+
+def test_supercell_too_small_is_rejected():
+    with pytest.raises(ValueError):
+        fcc_settings(1, 4, 2, 1, ["Al", "Mg"])
+
+
+def test_equivalent_decorations():
+    assert equivalent_decorations([0, 1], [[0, 1]]) == [[0, 1], [1, 0]]
+    assert equivalent_decorations([0, 0, 1], [[0, 1, 2]]) == [[0, 0, 1], [0, 1, 0], [1, 0, 0]]
+    assert equivalent_decorations([0, 1, 1], [[1, 2]]) == [[0, 1, 1]]
+    assert equivalent_decorations([1, 0, 1], []) == [[1, 0, 1]]
+    # every decoration's class contains it and classes partition the decorations
+    eq = [[0, 1, 2, 3]]
+    for deco in itertools.product(range(2), repeat=4):
+        cls = equivalent_decorations(list(deco), eq)
+        assert list(deco) in cls
+        assert all(sorted(c) == sorted(deco) for c in cls)
+
+
+def test_eci_names_sorted_and_parseable():
+    s = fcc_settings(4, 5, 3, 1, ["Al", "Mg", "Si"])
+    names = s.cset.names
+    assert names == sorted(names)
+    assert names[0] == "c0" and names[1] == "c1_0" and names[2] == "c1_1"
+    assert len(names) == 63
+    for n in names[3:]:
+        prefix, deco = n.rsplit("_", 1)
+        assert prefix in s.cluster_info[0]
+        assert len(deco) == s.cluster_info[0][prefix]["size"]
+
+
+def test_seeded_ecis_recipe():
+    s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
+    e1 = seeded_ecis(s.cset, 0)
+    e2 = seeded_ecis(s.cset, 0)
+    assert e1 == e2 and e1["c0"] == -3.0
+    assert seeded_ecis(s.cset, 1) != e1
+
+
+def test_model_terms_and_weights():
+    s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    assert m.n_terms == 122 and m.n_cols == 54
+    assert np.all(np.diff(m.term_eci) >= 0)
+    n = m.n_sites
+    for k, name in enumerate(m.eci_names):
+        if m.eci_kind[k] == 2:
+            t = m.eci_type[k]
+            size = m.type_size[t]
+            assert m.eci_weight[k] == pytest.approx(size / (m.type_M[t] * n))
+            assert m.eci_full_weight[k] == pytest.approx(1.0 / (m.type_M[t] * n))
+
+
+def test_model_from_sparse_translation_matrix_matches_dense():
+    """The list-of-dicts translation matrix (the reference's sparse form) gives the same table."""
+    s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m1 = CEModel(s, list(eci))
+
+    class Plain:
+        pass
+
+    p = Plain()
+    for attr in ("unique_elements", "num_unique_elements", "index_by_trans_symm", "background_indices",
+                 "cluster_info", "basis_functions", "trans_matrix"):
+        setattr(p, attr, getattr(s, attr))
+    m2 = CEModel(p, list(eci))
+    assert np.array_equal(m1.table, m2.table)
+    assert np.array_equal(m1.term_nb, m2.term_nb)
+    dense = np.zeros((s.n_sites, int(s.column_sites.max()) + 1), dtype=np.int32)
+    dense[:, s.column_sites] = s.table
+    p.trans_matrix = dense
+    m3 = CEModel(p, list(eci))
+    assert np.array_equal(m1.table, m3.table)
+
+
+def test_model_rejects_unknown_eci():
+    s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
+    with pytest.raises(ValueError):
+        CEModel(s, ["c0", "c1_0", "c7_d9999_0_0000000"])
