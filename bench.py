@@ -246,7 +246,7 @@ def run_gpu(args):
     bytes_per_flip = 5 * m.n_cols + 1
     keys = np.arange(N_CHAINS) + rank * N_CHAINS
     runner = BatchRunner(geo, occ, ev, Ts, E.MOVE_FLIP, seed=2026, precision=E.PREC_F32, warps=args.warps,
-                         sweeps_per_step=SWEEPS_PER_STEP, recompute_every=1, graph=True, chain_keys=keys)
+                         sweeps_per_step=args.sweeps_per_step, recompute_every=1, graph=True, chain_keys=keys)
     stream = runner.stream
     runner.capture()
     trials_per_step = N_CHAINS * runner.trials_per_step
@@ -281,6 +281,14 @@ def run_gpu(args):
     value = total_trials / t_max
     clocks = clk.summary()
     thermo = runner.thermodynamics()
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_case": True, "value": value, "unit": UNIT, "ms_per_step": t_max * 1e3 / args.steps,
+                              "warps_per_chain": runner.warps, "sweeps_per_step": args.sweeps_per_step}))
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
 
     # -- roofline of the dominant kernel: the MC launch alone, timed on its stream --------
     cb = runner.cb
@@ -354,7 +362,7 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "sgc_flip_fcc_binary_16x16x16_64chains", "n_sites": m.n_sites,
-                       "n_chains": N_CHAINS, "sweeps_per_step": SWEEPS_PER_STEP, "recompute": "fp64 every step",
+                       "n_chains": N_CHAINS, "sweeps_per_step": args.sweeps_per_step, "recompute": "fp64 every step",
                        "warps_per_chain": runner.warps, "cuda_graph": True,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
             "gpu_launches": n_launches,
@@ -385,6 +393,9 @@ def main(argv=None):
     p.add_argument("--warps", type=int, default=0, help="warps per chain (0 = autotuned)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)
+    p.add_argument("--profile", action="store_true",
+                   help="profiling case: the timed steps only (no end-to-end, plain-GPU or CPU legs)")
     args = p.parse_args(argv)
     if args.warmup < 3:
         p.error("at least 3 warm-up steps")

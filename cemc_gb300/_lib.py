@@ -49,7 +49,8 @@ class RunDesc(C.Structure):
                 ("seed", C.c_uint64), ("n_trials", C.c_uint64),
                 ("occ", _P), ("cf", _P), ("energy", _P), ("eci", _P), ("kT", _P), ("trial", _P), ("accum", _P),
                 ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
-                ("trace_site", _P), ("trace_acc", _P), ("trace_de", _P), ("status", _P), ("chain_key", _P)]
+                ("trace_site", _P), ("trace_acc", _P), ("trace_de", _P), ("status", _P), ("chain_key", _P),
+                ("accum_slot", _P), ("chain_trials", _P)]
 
 
 class CemcError(RuntimeError):
@@ -90,7 +91,7 @@ def load():
         L.cemc_energy.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
         L.cemc_apply_changes.argtypes = [_P, _P, _P, _P, _P, C.c_int32, _P, _P, _P, _P, _P]
         L.cemc_delta_e.argtypes = [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]
-        L.cemc_pt_exchange.argtypes = [C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, _P, _P, _P, _P, _P]
+        L.cemc_pt_exchange.argtypes = [C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, _P, _P, _P, _P, _P, _P]
         L.cemc_last_error.argtypes = [C.c_char_p, C.c_size_t]
         L.cemc_version.argtypes = [C.POINTER(C.c_int32)] * 3
         for name in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_run", "cemc_recompute", "cemc_energy",

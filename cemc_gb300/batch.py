@@ -77,7 +77,8 @@ class BatchRunner:
             if self.use_graph and self.recompute_every == 1:
                 if self._graph is None:
                     self.capture()
-                self._graph.replay()
+                with torch.cuda.stream(self.stream):  # replay() launches on the current stream
+                    self._graph.replay()
             else:
                 with torch.cuda.stream(self.stream):
                     rec = self.recompute_every > 0 and self.steps_done % self.recompute_every == 0

@@ -279,6 +279,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   a.trace_de = r->trace_de;
   a.status = r->status;
   a.chain_key = r->chain_key;
+  a.accum_slot = r->accum_slot;
+  a.chain_trials = r->chain_trials;
   // Shared memory: the occupation, then (swaps) the site lists, then an exact
   // stamp table (one entry per site) are preferred; fall back in that order.
   const size_t budget = (size_t)geo->max_smem;
@@ -313,6 +315,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   for (uint64_t done = 0; done < r->n_trials;) {
     const uint64_t n = std::min(max_chunk, r->n_trials - done);
     a.n_trials = n;
+    a.chunk_offset = done;
     cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "Monte Carlo kernel launch");
     done += n;
@@ -372,11 +375,11 @@ extern "C" int cemc_delta_e(const cemc_geometry *geo, const int8_t *occ, const d
 }
 
 extern "C" int cemc_pt_exchange(int32_t n_replicas, int32_t direction, uint64_t seed, uint64_t round,
-                                const double *energy, double *kT, int32_t *replica_of, int32_t *n_accept,
-                                void *stream) {
+                                const double *energy, double *kT, int32_t *replica_of, int32_t *position_of,
+                                int32_t *n_accept, void *stream) {
   if (n_replicas < 1 || !energy || !kT || !replica_of || (direction != 0 && direction != 1))
     return fail(CEMC_ERR_ARG, "bad replica-exchange arguments");
-  cudaError_t e = cemc::launch_pt(n_replicas, direction, seed, round, energy, kT, replica_of, n_accept,
+  cudaError_t e = cemc::launch_pt(n_replicas, direction, seed, round, energy, kT, replica_of, position_of, n_accept,
                                   static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "replica-exchange kernel launch");
   return CEMC_OK;

@@ -252,7 +252,7 @@ __global__ void delta_e_kernel(DevGeo g, const int8_t *occ, const double *eci, i
 // u < exp((1/kT_1 - 1/kT_2) (E_1 - E_2)) (parallel_tempering.py:138-144,167).
 // The two chains exchange temperatures and ladder positions.
 __global__ void pt_exchange_kernel(int n, int direction, uint64_t seed, uint64_t round, const double *energy,
-                                   double *kT, int32_t *replica_of, int32_t *n_accept) {
+                                   double *kT, int32_t *replica_of, int32_t *position_of, int32_t *n_accept) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   int acc_count = 0;
   if (direction == 0) {
@@ -293,6 +293,8 @@ __global__ void pt_exchange_kernel(int n, int direction, uint64_t seed, uint64_t
     }
   }
   if (n_accept) *n_accept = acc_count;
+  if (position_of)
+    for (int p = 0; p < n; ++p) position_of[replica_of[p]] = p;
 }
 
 // ---------------------------------------------------------------------------
@@ -337,8 +339,8 @@ cudaError_t launch_energy(const DevGeo &g, int n_chains, const double *eci, cons
 }
 
 cudaError_t launch_pt(int n, int direction, uint64_t seed, uint64_t round, const double *energy, double *kT,
-                      int32_t *replica_of, int32_t *n_accept, cudaStream_t st) {
-  pt_exchange_kernel<<<1, 32, 0, st>>>(n, direction, seed, round, energy, kT, replica_of, n_accept);
+                      int32_t *replica_of, int32_t *position_of, int32_t *n_accept, cudaStream_t st) {
+  pt_exchange_kernel<<<1, 32, 0, st>>>(n, direction, seed, round, energy, kT, replica_of, position_of, n_accept);
   return cudaGetLastError();
 }
 

@@ -68,18 +68,24 @@ __device__ __forceinline__ R warp_scan_incl(R v, int lane) {
 }
 
 // Metropolis test of the reference, accept = (dE < 0) or (u <= exp(-dE / kT))
-// (cemc/mcmc/montecarlo.py:950-956).  The comparison is first made as
-// ln(u) + dE/kT against a margin in single precision on the special-function
-// unit; only trials within the margin of the threshold evaluate the exact
-// double-precision form, so the decision equals the double-precision one.
-__device__ __forceinline__ int metropolis(double de, double u, double kT, float inv_kT) {
-  if (de < 0.0) return 1;
+// (cemc/mcmc/montecarlo.py:950-956), with u the 53-bit uniform of words (a, b).
+// The test is first made in single precision as ln(u) + dE/kT against a
+// margin that bounds every single-precision error involved: u is taken as
+// a * 2^-32 (within 2^-27 of the 53-bit u), ln on the special-function unit,
+// x = dE/kT rounded to float.  Only trials inside the margin evaluate the
+// exact double-precision form, so the decision equals the double-precision
+// one while the common case issues no FP64 instruction (the FP64 pipe of this
+// part is narrow).
+template <typename R>
+__device__ __forceinline__ int metropolis(R de, uint32_t ua, uint32_t ub, double kT, float inv_kT) {
+  if (de < (R)0) return 1;
   const float x = (float)de * inv_kT;
-  const float y = __logf((float)u) + x;
-  const float margin = 1e-4f + 1e-6f * x;
+  const float uf = (float)ua * 2.3283064e-10f;  // a * 2^-32
+  const float y = __logf(uf) + x;
+  const float margin = 1e-4f + 1e-6f * x + 1e-8f / uf;  // uf == 0 gives an infinite margin
   if (y < -margin) return 1;
   if (y > margin) return 0;
-  return u <= exp(-de / kT);
+  return cemc_u01_53(ua, ub) <= exp(-(double)de / kT);
 }
 
 // Fill one warp's vals array for a change of `site` from species `old_s` to

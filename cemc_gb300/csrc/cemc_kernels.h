@@ -18,6 +18,6 @@ cudaError_t launch_delta(const DevGeo &g, const int8_t *occ, const double *eci, 
 cudaError_t launch_energy(const DevGeo &g, int n_chains, const double *eci, const double *cf, double *energy,
                           cudaStream_t st);
 cudaError_t launch_pt(int n, int direction, uint64_t seed, uint64_t round, const double *energy, double *kT,
-                      int32_t *replica_of, int32_t *n_accept, cudaStream_t st);
+                      int32_t *replica_of, int32_t *position_of, int32_t *n_accept, cudaStream_t st);
 
 }  // namespace cemc

@@ -26,6 +26,9 @@ struct RunArgs {
   double *trace_de;
   int32_t *status;
   const uint32_t *chain_key;
+  const int32_t *accum_slot;
+  const uint64_t *chain_trials;
+  uint64_t chunk_offset;  // trials of this chain already run by earlier chunks of the same call
 };
 
 constexpr int kRing = 128;     // trial slots of the draw / row ring (power of two, > 3 * kMaxEval)
@@ -80,8 +83,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   L.rec_tsb = 4 * 32;
   L.rec_acc = 8 * 32;
   L.rec_der = align16(L.rec_acc + 32);
-  L.rec_de = align16(L.rec_der + (size_t)rsize * 32);
-  L.rec_d = align16(L.rec_de + 8 * 32);
+  L.rec_de = L.rec_der;  // unused
+  L.rec_d = align16(L.rec_der + (size_t)rsize * 32);
   L.rec_stride = align16(L.rec_d + (size_t)rsize * 32 * K);
   L.rec = o;
   o = align16(o + 2 * L.rec_stride);

@@ -161,9 +161,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   const double kT = a.kT[chain];
   const float inv_kT = (float)(1.0 / kT);
   const uint32_t key = a.chain_key ? a.chain_key[chain] : (uint32_t)chain;
+  uint64_t my_trials = a.n_trials;
+  if (a.chain_trials) {
+    // this chunk covers trials [chunk_offset, chunk_offset + n_trials) of the call
+    const uint64_t total = a.chain_trials[chain];
+    my_trials = total <= a.chunk_offset ? 0 : (total - a.chunk_offset < a.n_trials ? total - a.chunk_offset : a.n_trials);
+  }
   const uint64_t t_first = a.trial[chain];
-  const uint64_t t_end = t_first + a.n_trials;
-  const double e_ref = a.accum ? a.accum[chain].e_ref : 0.0;
+  const uint64_t t_end = t_first + my_trials;
+  const int acc_row = a.accum_slot ? a.accum_slot[chain] : chain;
+  const double e_ref = a.accum ? a.accum[acc_row].e_ref : 0.0;
 
   // Helper-warp state.
   double energy = a.energy[chain];
@@ -269,7 +276,6 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     int32_t *tsb = reinterpret_cast<int32_t *>(rec + L.rec_tsb);
     int8_t *tacc = reinterpret_cast<int8_t *>(rec + L.rec_acc);
     R *tder = reinterpret_cast<R *>(rec + L.rec_der);
-    double *tde = reinterpret_cast<double *>(rec + L.rec_de);
     R *tD = reinterpret_cast<R *>(rec + L.rec_d);
     if (!helper) {
       // ---- phase A: every evaluating warp computes one trial speculatively ----
@@ -278,14 +284,15 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
         const int slot = (int)(t & (kRing - 1));
         const Draw dr = draws[slot];
         int sa, sb = -1, na;
-        int nbra[4], nbrb[4];
-        double u = 0.0;
+        int nbra[4], nbrb[4] = {-1, -1, -1, -1};
+        uint32_t ua, ub;
         if (!SWAP) {
           sa = dr.site;
           const int oa = occ[sa];
           const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
           na = k + (k >= oa);
-          if (lane == 0) u = cemc_u01_53(dr.w2, dr.w3);
+          ua = dr.w2;
+          ub = dr.w3;
           gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
         } else {
           const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
@@ -295,7 +302,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
           sa = trk[misc[12 + A] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A])];
           sb = trk[misc[12 + B] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B])];
           na = B;
-          if (lane == 0) u = cemc_u01_53(dr.x0, dr.x1);
+          ua = dr.x0;
+          ub = dr.x1;
           // first half: site a takes B; second half: site b takes A with a already changed
           gather_vals<R>(g, occ, bf_s, sa, A, B, -1, 0, va, nbra, lane);
           gather_vals<R>(g, occ, bf_s, sb, B, A, sa, B, vb, nbrb, lane);
@@ -307,12 +315,11 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
                                           tD + (size_t)warp * n_eci, lane);
         int acc = 0;
         if (lane == 0) {
-          acc = metropolis((double)de, u, kT, inv_kT);
+          acc = metropolis<R>(de, ua, ub, kT, inv_kT);
           tsa[warp] = sa;
           tsb[warp] = SWAP ? sb : na;
           tacc[warp] = (int8_t)acc;
           tder[warp] = de;
-          tde[warp] = (double)de;
         }
         acc = __shfl_sync(kFull, acc, 0);
         if (acc) {
@@ -371,7 +378,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
         a.trace_site[2 * idx] = tsa[lane];
         a.trace_site[2 * idx + 1] = tsb[lane];
         a.trace_acc[idx] = tacc[lane];
-        a.trace_de[idx] = tde[lane];
+        a.trace_de[idx] = (double)tder[lane];
       }
       if (lane == 0) misc[0] = ks;
     }
@@ -408,7 +415,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     a.energy[chain] = e * (double)(unsigned)N;
     a.trial[chain] = t_end;
     if (a.accum) {
-      cemc_accum *ac = a.accum + chain;
+      cemc_accum *ac = a.accum + acc_row;
       ac->sum_e += acc_s[0];
       ac->sum_e2 += acc_s[1];
       for (int b = 0; b < g.n_bf; ++b) {
@@ -416,7 +423,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
         ac->sum_s2[b] += acc_s[2 + CEMC_MAX_BF + b];
         ac->sum_se[b] += acc_s[2 + 2 * CEMC_MAX_BF + b];
       }
-      ac->n_samples += a.n_trials;
+      ac->n_samples += my_trials;
       ac->n_accept += n_acc_launch;
     }
     if (a.status) a.status[chain] = 0;

@@ -173,9 +173,60 @@ class ChainBatch:
         self.recompute()
         self.reset_accumulators()
 
+    @classmethod
+    def wrap(cls, geo: Geometry, occ: torch.Tensor, cf: torch.Tensor, energy: torch.Tensor, eci: torch.Tensor,
+             kT, move: int, seed: int = 0, chain_key: int = 0, stream=None) -> "ChainBatch":
+        """One chain over EXISTING device tensors (no copies): occ (N,), cf (n_eci,), energy (1,), eci (n_eci,).
+
+        Used by the drop-in drivers, whose calculator already holds the state on the device.
+        """
+        self = cls.__new__(cls)
+        m = geo.model
+        dev = occ.device
+        self.geo = geo
+        self.n_chains = 1
+        self.move = int(move)
+        self.seed = int(seed)
+        self.stream = stream
+        self.occ = occ.view(1, m.n_sites)
+        self.cf = cf.view(1, m.n_eci)
+        self.energy = energy.view(1)
+        self.eci = eci.view(1, m.n_eci)
+        self.kT = torch.tensor([float(kT)], dtype=torch.float64, device=dev)
+        self.trial = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.accum = torch.zeros((1, ACCUM_DOUBLES), dtype=torch.float64, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.chain_key = torch.tensor([int(chain_key)], dtype=torch.int32, device=dev)
+        self.trk = self.loc = self.trk_start = self.trk_count = None
+        if self.move == MOVE_SWAP:
+            self.rebuild_tracker()
+        self.scratch = torch.empty(max(geo.scratch_doubles(1), 1), dtype=torch.float64, device=dev)
+        self.reset_accumulators()
+        return self
+
+    def rebuild_tracker(self):
+        """Per-species site lists from the current occupation (after external changes)."""
+        m = self.geo.model
+        occ = self.occ.cpu().numpy()
+        trk, loc, start, count = build_tracker(occ, m.n_sym)
+        if np.any((count > 0).sum(axis=1) < 2):
+            raise ValueError("swap moves need at least two species present in every chain")
+        dev = self.occ.device
+        self.trk = torch.as_tensor(trk).to(dev)
+        self.loc = torch.as_tensor(loc).to(dev)
+        self.trk_start = torch.as_tensor(start).to(dev)
+        self.trk_count = torch.as_tensor(count).to(dev)
+
+    def set_temperature(self, kT):
+        self.kT.copy_(torch.as_tensor(np.broadcast_to(np.asarray(kT, dtype=np.float64), (self.n_chains,)).copy()))
+
     # -- library calls -----------------------------------------------------
-    def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False):
-        """Run ``n_trials`` trials on every chain in one launch (``cemc_run``)."""
+    def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
+            chain_trials: Optional[torch.Tensor] = None):
+        """Run ``n_trials`` trials on every chain in one launch (``cemc_run``).
+
+        ``chain_trials`` (device int64, one per chain, each <= n_trials) gives chains their own counts.
+        """
         tr = None
         if trace:
             tr = (torch.zeros(self.n_chains * n_trials * 2, dtype=torch.int32, device=self.occ.device),
@@ -186,7 +237,8 @@ class ChainBatch:
                          _ptr(self.kT), _ptr(self.trial), _ptr(self.accum), _ptr(self.trk), _ptr(self.loc),
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
-                         _ptr(self.status), _ptr(self.chain_key))
+                         _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
+                         _ptr(chain_trials))
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         if trace:
@@ -237,7 +289,8 @@ class ChainBatch:
 
 
 def pt_exchange(energy: torch.Tensor, kT: torch.Tensor, replica_of: torch.Tensor, direction: int, seed: int,
-                round_index: int, n_accept: Optional[torch.Tensor] = None, stream=None):
+                round_index: int, n_accept: Optional[torch.Tensor] = None, stream=None,
+                position_of: Optional[torch.Tensor] = None):
     """One replica-exchange sweep over a ladder on the device (``cemc_pt_exchange``).
 
     ``replica_of[pos]`` is the chain at ladder position ``pos``; accepted pairs
@@ -246,5 +299,6 @@ def pt_exchange(energy: torch.Tensor, kT: torch.Tensor, replica_of: torch.Tensor
     L = _lib.load()
     with torch.cuda.device(energy.device):
         _lib.check(L.cemc_pt_exchange(int(replica_of.numel()), int(direction), int(seed) & (2 ** 64 - 1),
-                                      int(round_index), _ptr(energy), _ptr(kT), _ptr(replica_of), _ptr(n_accept),
+                                      int(round_index), _ptr(energy), _ptr(kT), _ptr(replica_of),
+                                      _ptr(position_of), _ptr(n_accept),
                                       _stream_ptr(stream)))

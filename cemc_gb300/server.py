@@ -1,0 +1,325 @@
+"""Continuous-batching Monte Carlo job server on one GPU.
+
+The reference is a single-process library with no server; this module is the
+serving layer the batched kernels make possible.  Jobs (supercell, cluster
+recipe, ECIs, ensemble, temperature, chemical potential, sweep budget) arrive
+at any time.  Jobs that share a geometry (supercell size and cluster set)
+share a device-resident slot batch; each batch advances all of its occupied
+slots by one quantum per tick in ONE launch of the fused kernel on its own
+CUDA stream, so batches of different geometries overlap on the device.  A
+job is admitted as soon as a slot of its batch is free and its state fits the
+HBM budget; it leaves when its budget is spent, and its slot is reused at the
+next tick.
+
+A job's trials depend only on (seed, job key, trial index) and on its own
+state, and every quantum ends with the same FP64 recompute, so a job's result
+is the same whether it runs alone or in a mix (tested).
+"""
+from __future__ import annotations
+
+import itertools
+import math
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import engine as E
+from .batch import KB_EV
+from .lattice import fcc_settings, seeded_ecis
+from .tables import CEModel
+
+# Cluster recipes of the benchmark configurations: (pair shells, triplet shells, quad shells, species)
+RECIPES: Dict[str, Tuple[int, int, int, Tuple[str, ...]]] = {
+    "binary": (4, 2, 1, ("Al", "Mg")),
+    "binary6": (6, 2, 1, ("Al", "Mg")),
+    "ternary": (5, 3, 1, ("Al", "Mg", "Si")),
+}
+
+
+@dataclass
+class Job:
+    """One Monte Carlo job.
+
+    ``occ`` (species ids) defaults to a random configuration at ``composition``
+    (fractions per species, default equal); ``eci`` defaults to the seeded
+    recipe ECIs; ``mu`` is folded into ``c1_0`` for semi-grand-canonical jobs.
+    """
+
+    L: int
+    recipe: str = "binary"
+    ensemble: str = "sgc"  # "sgc" (flips) or "canonical" (swaps)
+    T: float = 800.0
+    mu: float = 0.0
+    sweeps: float = 100.0
+    seed: int = 0
+    eci: Optional[Dict[str, float]] = None
+    occ: Optional[np.ndarray] = None
+    composition: Optional[List[float]] = None
+    job_id: int = -1
+    arrival: float = 0.0
+    admitted: float = float("nan")
+    done: float = float("nan")
+    result: Optional[dict] = None
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+class _Group:
+    """Slots of one (geometry, move) pair resident on the device."""
+
+    def __init__(self, server: "MCServer", key, model: CEModel, geo: E.Geometry, move: int, capacity: int):
+        self.key = key
+        self.model = model
+        self.geo = geo
+        self.move = move
+        self.capacity = capacity
+        self.stream = torch.cuda.Stream(device=geo.device)
+        n = model.n_sites
+        occ = np.zeros((capacity, n), dtype=np.int8)
+        occ[:, : n // 2] = 1  # placeholder configurations (two species present) until slots fill
+        with torch.cuda.stream(self.stream):
+            self.cb = E.ChainBatch(geo, occ, np.zeros(model.n_eci), 1.0, move, seed=server.seed, stream=self.stream)
+        self.jobs: List[Optional[Job]] = [None] * capacity
+        self.remaining = np.zeros(capacity, dtype=np.int64)
+        self.chain_trials = torch.zeros(capacity, dtype=torch.int64, device=geo.device)
+        self.bytes_per_slot = n * (1 + (8 if move == E.MOVE_SWAP else 0)) + model.n_eci * 16 + 256
+        self.launched = False
+
+    def free_slot(self) -> int:
+        for i, j in enumerate(self.jobs):
+            if j is None:
+                return i
+        return -1
+
+    def active(self) -> int:
+        return sum(j is not None for j in self.jobs)
+
+
+class MCServer:
+    """Request loop: admit, tick, retire.
+
+    :param hbm_budget_gb: device memory the server may hold in chain state and tables.
+    :param quantum_sweeps: sweeps per job per tick (one launch per batch per tick).
+    :param capacity: slots per geometry batch.
+    """
+
+    def __init__(self, device="cuda", hbm_budget_gb: float = 120.0, quantum_sweeps: float = 10.0, capacity: int = 64,
+                 precision: int = E.PREC_F32, warps: int = 16, seed: int = 2026, kB: float = KB_EV):
+        self.device = E.require_cuda(device)
+        self.budget = hbm_budget_gb * 1e9
+        self.used = 0.0
+        self.quantum = float(quantum_sweeps)
+        self.capacity = int(capacity)
+        self.precision = precision
+        self.warps = warps
+        self.seed = int(seed)
+        self.kB = kB
+        self.groups: Dict[tuple, _Group] = {}
+        self.models: Dict[tuple, Tuple[CEModel, E.Geometry, dict]] = {}
+        self.pending: List[Job] = []
+        self.finished: List[Job] = []
+        self._ids = itertools.count()
+        self._lock = threading.Lock()
+        self.trials_done = 0
+        self.t_start = None
+
+    # -- submission ------------------------------------------------------------------
+    def submit(self, job: Job) -> Job:
+        with self._lock:
+            if job.job_id < 0:
+                job.job_id = next(self._ids)
+            if not job.arrival:
+                job.arrival = time.perf_counter()
+            self.pending.append(job)
+        return job
+
+    def _model(self, job: Job):
+        key = (job.L, job.recipe)
+        hit = self.models.get(key)
+        if hit is None:
+            ps, ts, qs, species = RECIPES[job.recipe]
+            s = fcc_settings(job.L, ps, ts, qs, list(species))
+            eci = seeded_ecis(s.cset, 0)
+            m = CEModel(s, list(eci))
+            geo = E.Geometry(m, self.device)
+            tbytes = m.n_sites * m.n_cols * 8 + m.n_terms * 16
+            self.used += tbytes
+            hit = (m, geo, eci)
+            self.models[key] = hit
+        return hit
+
+    def _job_state(self, job: Job, m: CEModel, default_eci: dict):
+        rng = np.random.default_rng(job.seed)
+        if job.occ is not None:
+            occ = np.asarray(job.occ, dtype=np.int8)
+        else:
+            comp = np.asarray(job.composition if job.composition is not None else [1.0] * m.n_sym, dtype=float)
+            comp = comp / comp.sum()
+            counts = np.floor(comp * m.n_sites).astype(int)
+            counts[0] += m.n_sites - counts.sum()
+            occ = np.repeat(np.arange(m.n_sym, dtype=np.int8), counts)
+            rng.shuffle(occ)
+        eci = dict(default_eci if job.eci is None else job.eci)
+        if job.ensemble == "sgc":
+            eci["c1_0"] = eci.get("c1_0", 0.0) - job.mu
+        return occ, m.eci_vector(eci)
+
+    def _admit(self):
+        """Place pending jobs (arrival order) into free slots while memory allows."""
+        with self._lock:
+            pending = list(self.pending)
+        admitted = []
+        for job in pending:
+            m, geo, eci0 = self._model(job)
+            move = E.MOVE_FLIP if job.ensemble == "sgc" else E.MOVE_SWAP
+            gkey = (job.L, job.recipe, move)
+            grp = self.groups.get(gkey)
+            if grp is None:
+                need = self.capacity * (m.n_sites * (9 if move == E.MOVE_SWAP else 1) + m.n_eci * 16 + 256)
+                if self.used + need > self.budget:
+                    continue
+                grp = _Group(self, gkey, m, geo, move, self.capacity)
+                self.groups[gkey] = grp
+                self.used += need
+            slot = grp.free_slot()
+            if slot < 0:
+                continue
+            occ, ev = self._job_state(job, m, eci0)
+            self._load_slot(grp, slot, job, occ, ev)
+            job.admitted = time.perf_counter()
+            admitted.append(job)
+        if admitted:
+            with self._lock:
+                ids = {j.job_id for j in admitted}
+                self.pending = [j for j in self.pending if j.job_id not in ids]
+
+    def _load_slot(self, grp: _Group, slot: int, job: Job, occ: np.ndarray, ev: np.ndarray):
+        cb = grp.cb
+        m = grp.model
+        with torch.cuda.stream(grp.stream):
+            cb.occ[slot].copy_(torch.as_tensor(occ))
+            cb.eci[slot].copy_(torch.as_tensor(ev))
+            cb.kT[slot] = self.kB * job.T
+            cb.trial[slot] = 0
+            # the stream of a job depends on its own seed only, never on its slot or arrival order
+            cb.chain_key[slot] = (job.seed * 2654435761 + 97) & 0x7FFFFFFF
+            if grp.move == E.MOVE_SWAP:
+                from .engine import build_tracker
+                trk, loc, start, count = build_tracker(occ[None], m.n_sym)
+                cb.trk[slot].copy_(torch.as_tensor(trk[0]))
+                cb.loc[slot].copy_(torch.as_tensor(loc[0]))
+                cb.trk_start[slot].copy_(torch.as_tensor(start[0]))
+                cb.trk_count[slot].copy_(torch.as_tensor(count[0]))
+            self._recompute_slot(grp, slot)
+            cb.accum[slot].zero_()
+            cb.accum[slot, E.A_EREF] = cb.energy[slot]
+        grp.jobs[slot] = job
+        grp.remaining[slot] = int(round(job.sweeps * m.n_sites))
+
+    def _recompute_slot(self, grp: _Group, slot: int):
+        cb = grp.cb
+        L = cb.geo.L
+        m = grp.model
+        el = 8
+        _lib.check(L.cemc_recompute(cb.geo.handle, 1, cb.occ.data_ptr() + slot * m.n_sites,
+                                    cb.eci.data_ptr() + slot * m.n_eci * el, cb.cf.data_ptr() + slot * m.n_eci * el,
+                                    cb.energy.data_ptr() + slot * el, cb.scratch.data_ptr(),
+                                    grp.stream.cuda_stream))
+
+    # -- the loop ----------------------------------------------------------------------
+    def _tick(self):
+        """Launch one quantum on every batch with active slots (each on its own stream)."""
+        launched = []
+        for grp in self.groups.values():
+            if grp.active() == 0:
+                continue
+            q = int(round(self.quantum * grp.model.n_sites))
+            per = np.minimum(grp.remaining, q)
+            per[[j is None for j in grp.jobs]] = 0
+            n_max = int(per.max())
+            if n_max == 0:
+                continue
+            with torch.cuda.stream(grp.stream):
+                grp.chain_trials.copy_(torch.as_tensor(per), non_blocking=False)
+                grp.cb.run(n_max, precision=self.precision, warps=self.warps, chain_trials=grp.chain_trials)
+                grp.cb.recompute()
+            grp.remaining -= per
+            self.trials_done += int(per.sum())
+            launched.append(grp)
+        return launched
+
+    def _retire(self, groups: List[_Group]):
+        for grp in groups:
+            grp.stream.synchronize()
+            grp.cb.check_status()
+            done = [i for i, j in enumerate(grp.jobs) if j is not None and grp.remaining[i] <= 0]
+            if not done:
+                continue
+            acc = grp.cb.accum_host()
+            energy = grp.cb.energy.cpu().numpy()
+            cf = grp.cb.cf.cpu().numpy()
+            kT = grp.cb.kT.cpu().numpy()
+            now = time.perf_counter()
+            for i in done:
+                job = grp.jobs[i]
+                a = acc[i]
+                n = max(a[E.A_NSAMP], 1.0)
+                mean = a[E.A_EREF] + a[E.A_SUM_E] / n
+                T = kT[i] / self.kB
+                job.result = {"energy": mean, "final_energy": float(energy[i]),
+                              "heat_capacity": (a[E.A_SUM_E2] / n - (a[E.A_SUM_E] / n) ** 2) / (self.kB * T * T),
+                              "singlet_c1_0": a[E.A_SUM_S] / n, "accept_rate": a[E.A_NACC] / n,
+                              "n_mc_steps": int(a[E.A_NSAMP]), "cf": cf[i].copy(),
+                              "occupation": grp.cb.occ[i].cpu().numpy().copy()}
+                job.done = now
+                grp.jobs[i] = None
+                self.finished.append(job)
+
+    def step(self) -> int:
+        """Admit, tick, retire once; returns the number of active jobs."""
+        if self.t_start is None:
+            self.t_start = time.perf_counter()
+        self._admit()
+        launched = self._tick()
+        self._retire(launched)
+        return sum(g.active() for g in self.groups.values())
+
+    def run_until_idle(self, max_ticks: int = 10 ** 9):
+        for _ in range(max_ticks):
+            active = self.step()
+            with self._lock:
+                waiting = len(self.pending)
+            if active == 0 and waiting == 0:
+                break
+
+    def stats(self) -> dict:
+        lat = np.array([j.latency for j in self.finished]) if self.finished else np.zeros(1)
+        wall = (time.perf_counter() - self.t_start) if self.t_start else 0.0
+        return {"jobs": len(self.finished), "p50_latency_s": float(np.percentile(lat, 50)),
+                "p99_latency_s": float(np.percentile(lat, 99)), "trials": self.trials_done,
+                "trials_per_s": self.trials_done / wall if wall > 0 else 0.0, "wall_s": wall,
+                "hbm_used_gb": self.used / 1e9}
+
+
+def poisson_stream(n_jobs: int, rate: float, seed: int = 0, L_range=(4, 32), sweeps_range=(1e2, 1e4),
+                   T_range=(300.0, 1200.0), recipes=("binary", "ternary", "binary6"), mu_range=(-0.2, 0.2)):
+    """Synthetic served stream: Poisson arrivals, log-uniform supercells and budgets, uniform T."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    jobs = []
+    for i in range(n_jobs):
+        t += rng.exponential(1.0 / rate)
+        L = int(round(math.exp(rng.uniform(math.log(L_range[0]), math.log(L_range[1])))))
+        sweeps = float(math.exp(rng.uniform(math.log(sweeps_range[0]), math.log(sweeps_range[1]))))
+        recipe = recipes[int(rng.integers(len(recipes)))]
+        ens = "sgc" if rng.random() < 0.5 else "canonical"
+        jobs.append(Job(L=max(L, 4), recipe=recipe, ensemble=ens, T=float(rng.uniform(*T_range)),
+                        mu=float(rng.uniform(*mu_range)), sweeps=sweeps, seed=i + 1, arrival=t))
+    return jobs

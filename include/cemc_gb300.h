@@ -128,6 +128,10 @@ typedef struct {
   double *trace_de;
   int32_t *status;     /* [n_chains] device status words, may be NULL */
   const uint32_t *chain_key; /* [n_chains] RNG key of each chain (device), NULL = chain index */
+  const int32_t *accum_slot; /* [n_chains] row of `accum` each chain adds to (device), NULL = chain index;
+                                lets a temperature ladder keep its sums per temperature */
+  const uint64_t *chain_trials; /* [n_chains] trials of each chain in this launch (device, each <= n_trials),
+                                   NULL = n_trials for every chain; lets a batch mix jobs with different budgets */
 } cemc_run_desc;
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
@@ -174,9 +178,11 @@ int cemc_delta_e(const cemc_geometry *geo, const int8_t *occ, const double *eci,
  * (i, i+1) of ladder positions starting at parity `direction`, accepted when
  * u < exp((1/kT_i - 1/kT_j)(E_i - E_j)).  Temperatures are exchanged, not
  * configurations: replica_of[pos] names the chain at ladder position pos and
- * is permuted in place; kT[chain] is rewritten accordingly. */
+ * is permuted in place; kT[chain] is rewritten accordingly, and position_of
+ * (may be NULL) receives the inverse permutation, position_of[chain] = pos. */
 int cemc_pt_exchange(int32_t n_replicas, int32_t direction, uint64_t seed, uint64_t round,
-                     const double *energy, double *kT, int32_t *replica_of, int32_t *n_accept, void *stream);
+                     const double *energy, double *kT, int32_t *replica_of, int32_t *position_of, int32_t *n_accept,
+                     void *stream);
 
 /* Message of the last failure on this thread. */
 int cemc_last_error(char *buf, size_t len);

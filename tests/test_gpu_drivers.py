@@ -1,0 +1,230 @@
+"""Drop-in calculator and drivers on the GPU: the reference's call sequences, its test invariants, serving."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import KB, golden_model, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")), seed=0, eci_seed=0):
+    from cemc_gb300.calculator import CE, SimpleAtoms
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    L, ps, ts, qs, syms = recipe
+    s = fcc_settings(L, ps, ts, qs, list(syms))
+    eci = seeded_ecis(s.cset, eci_seed)
+    rng = np.random.default_rng(seed)
+    symbols = [syms[i] for i in rng.integers(0, len(syms), s.n_sites)]
+    atoms = SimpleAtoms(symbols)
+    calc = CE(atoms, s, eci=dict(eci))
+    return atoms, calc, s, eci
+
+
+def test_calculator_swap_sequences_match_full_recompute(torch_cuda, oracle_mod):
+    """tests/test_CE_updater.py:86-115 (double swaps): incremental cf == brute force after each swap."""
+    atoms, calc, s, eci = _calc(recipe=(4, 5, 3, 1, ("Al", "Mg", "Si")))
+    m = calc.model
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(1)
+    for _ in range(15):
+        i1 = int(rng.integers(m.n_sites))
+        s1 = atoms[i1].symbol
+        i2, s2 = i1, s1
+        while s2 == s1:
+            i2 = int(rng.integers(m.n_sites))
+            s2 = atoms[i2].symbol
+        e = calc.calculate(atoms, ["energy"], [(i1, s1, s2), (i2, s2, s1)])
+        cf = calc.get_cf()
+        brute = orc.full_cf(m.occupation([a.symbol for a in atoms]))
+        assert np.allclose([cf[k] for k in m.eci_names], brute, rtol=1e-9, atol=1e-13)
+        assert e == pytest.approx(orc.energy(m.eci_vector(eci), brute), rel=1e-9)
+        calc.clear_history()
+
+
+def test_calculator_undo_restores_state(torch_cuda):
+    atoms, calc, s, eci = _calc()
+    cf0 = calc.get_cf()
+    e0 = calc.get_energy()
+    sym0 = [a.symbol for a in atoms]
+    calc.calculate(atoms, ["energy"], [(0, atoms[0].symbol, "Mg" if atoms[0].symbol == "Al" else "Al")])
+    calc.calculate(atoms, ["energy"], [(5, atoms[5].symbol, "Mg" if atoms[5].symbol == "Al" else "Al")])
+    calc.calculate(atoms, ["energy"], [(0, atoms[0].symbol, "Mg" if atoms[0].symbol == "Al" else "Al")])
+    assert calc.get_energy() != e0
+    calc.undo_changes()
+    assert [a.symbol for a in atoms] == sym0
+    assert calc.get_cf() == cf0 and calc.get_energy() == e0
+
+
+def test_calculator_rejects_inconsistent_move(torch_cuda):
+    atoms, calc, s, eci = _calc()
+    wrong = "Mg" if atoms[3].symbol == "Al" else "Al"
+    with pytest.raises(RuntimeError):
+        calc.calculate(atoms, ["energy"], [(3, wrong, atoms[3].symbol)])
+
+
+def test_calculator_singlets_update_ecis_and_set_symbols(torch_cuda, oracle_mod):
+    atoms, calc, s, eci = _calc()
+    m = calc.model
+    sing = calc.get_singlets()
+    occ = m.occupation([a.symbol for a in atoms])
+    assert sing[0] == pytest.approx(np.mean(np.where(occ == 0, 1.0, -1.0)), abs=1e-14)
+    new = dict(eci)
+    new["c1_0"] += 0.05
+    calc.update_ecis(new)
+    cf = calc.get_cf()
+    assert calc.get_energy() == pytest.approx(m.n_sites * sum(new[k] * cf[k] for k in m.eci_names), rel=1e-12)
+    calc.set_composition({"Al": 0.75, "Mg": 0.25})
+    assert sum(a.symbol == "Mg" for a in atoms) == m.n_sites // 4
+    orc = oracle_mod.Oracle(m)
+    brute = orc.full_cf(m.occupation([a.symbol for a in atoms]))
+    assert np.allclose([calc.get_cf()[k] for k in m.eci_names], brute, atol=1e-13)
+
+
+def test_montecarlo_runmc_accounting_and_thermodynamics(torch_cuda, oracle_mod):
+    from cemc_gb300.mcmc import Montecarlo
+    atoms, calc, s, eci = _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")))
+    c0 = calc.eci["c0"]
+    mc = Montecarlo(atoms, 600.0, seed=5)
+    mc.runMC(mode="fixed", steps=5000, equil=False)
+    q = mc.get_thermodynamic()
+    for key in ("energy", "heat_capacity", "energy_std", "temperature", "Al_conc", "Mg_conc"):
+        assert key in q
+    assert mc.current_step == 5000
+    assert calc.eci["c0"] == pytest.approx(c0, abs=1e-12)  # bias added back (montecarlo.py:213-217)
+    # composition is conserved by swaps; energy consistent with a recompute
+    m = calc.model
+    orc = oracle_mod.Oracle(m)
+    occ = calc.updater.occupation()
+    assert np.array_equal(occ, m.occupation([a.symbol for a in atoms]))
+    brute = orc.full_cf(occ)
+    assert calc.get_energy() == pytest.approx(orc.energy(m.eci_vector(calc.eci), brute), rel=1e-9)
+    assert q["heat_capacity"] >= 0.0
+
+
+def test_montecarlo_equilibration_and_prec_mode(torch_cuda):
+    from cemc_gb300.mcmc import Montecarlo
+    atoms, calc, s, eci = _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")))
+    mc = Montecarlo(atoms, 2000.0, seed=7)
+    mc.runMC(mode="prec", steps=20000, equil=True, prec=1.0)
+    q = mc.get_thermodynamic()
+    assert np.isfinite(q["energy"]) and mc.current_step <= 20000
+
+
+def test_sgc_runmc_and_thermodynamics(torch_cuda):
+    from cemc_gb300.mcmc import SGCMonteCarlo
+    atoms, calc, s, eci = _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")))
+    c1 = calc.eci["c1_0"]
+    mc = SGCMonteCarlo(atoms, 800.0, seed=3)
+    mc.runMC(mode="fixed", steps=8000, chem_potential={"c1_0": 0.15}, equil=False)
+    q = mc.get_thermodynamic()
+    for key in ("sgc_energy", "sgc_heat_capacity", "energy", "temperature", "n_mc_steps", "singlet_c1_0",
+                "var_singlet_c1_0", "mu_c1_0", "Al_conc", "Mg_conc"):
+        assert key in q, key
+    assert q["n_mc_steps"] == 8000
+    assert q["Al_conc"] + q["Mg_conc"] == pytest.approx(1.0)
+    assert calc.eci["c1_0"] == pytest.approx(c1, abs=1e-12)  # chemical potential removed again
+    # energy = sgc_energy + mu * <singlet> * N (sgc_montecarlo.py:419-422)
+    assert q["energy"] == pytest.approx(q["sgc_energy"] + 0.15 * q["singlet_c1_0"] * len(atoms), rel=1e-12)
+
+
+def test_sgc_chemical_potential_shifts_composition(torch_cuda):
+    """A positive mu on c1_0 favours the species with bf = +1 (thermodynamic sanity, sgc_montecarlo.py:239-261)."""
+    from cemc_gb300.mcmc import SGCMonteCarlo
+    res = []
+    for mu in (-0.3, 0.3):
+        atoms, calc, s, eci = _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")), seed=4)
+        mc = SGCMonteCarlo(atoms, 1000.0, seed=11)
+        mc.runMC(steps=20000, chem_potential={"c1_0": mu}, equil=False)
+        res.append(mc.get_thermodynamic()["singlet_c1_0"])
+    assert res[1] > res[0]
+
+
+def test_parallel_tempering_ladder(torch_cuda):
+    from cemc_gb300 import engine as E
+    from cemc_gb300.parallel_tempering import ParallelTempering
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m)
+    occ = np.zeros(m.n_sites, dtype=np.int8)
+    occ[: m.n_sites // 2] = 1
+    pt = ParallelTempering(geo, occ, m.eci_vector(eci), temperatures=np.geomspace(200, 1500, 8), seed=1, warps=8)
+    pt.run(sweeps_per_cycle=2, num_exchange_cycles=6, record=True)
+    lad = pt.ladder()
+    assert sorted(x["chain"] for x in lad) == list(range(8))
+    kT = pt.cb.kT.cpu().numpy()
+    for x in lad:
+        assert kT[x["chain"]] == pytest.approx(KB * x["temperature"])
+        assert x["n_mc_steps"] == 6 * 2 * m.n_sites
+    assert sum(pt.accepted_exchanges) > 0
+    # composition conserved in every replica (canonical swaps)
+    assert np.all(pt.cb.occ.cpu().numpy().sum(axis=1) == m.n_sites // 2)
+
+
+def test_server_result_same_alone_and_in_a_mix(torch_cuda):
+    """North-star serving property: a job's result does not depend on what else is on the GPU."""
+    from cemc_gb300.server import Job, MCServer
+    def make(seed, L=4, recipe="binary", ens="sgc", sweeps=30):
+        return Job(L=L, recipe=recipe, ensemble=ens, T=700.0, mu=0.05, sweeps=sweeps, seed=seed)
+    alone = MCServer(quantum_sweeps=7, capacity=8)
+    a = alone.submit(make(42))
+    alone.run_until_idle()
+    mixed = MCServer(quantum_sweeps=7, capacity=8)
+    others = [make(100 + i, L=4 + (i % 2), recipe=("binary", "ternary")[i % 2], ens=("sgc", "canonical")[i % 2],
+                   sweeps=10 + 13 * i) for i in range(9)]
+    for j in others[:4]:
+        mixed.submit(j)
+    b = mixed.submit(make(42))
+    mixed.step()
+    for j in others[4:]:
+        mixed.submit(j)
+    mixed.run_until_idle()
+    assert a.result is not None and b.result is not None
+    assert np.array_equal(a.result["occupation"], b.result["occupation"])
+    assert np.array_equal(a.result["cf"], b.result["cf"])
+    assert a.result["energy"] == b.result["energy"]
+    st = mixed.stats()
+    assert st["jobs"] == 10 and st["p99_latency_s"] >= st["p50_latency_s"] > 0
+    for j in others:
+        assert j.result["n_mc_steps"] == int(round(j.sweeps * (4 * j.L ** 3)))
+
+
+def test_fp32_drift_and_recompute_at_benchmark_size(torch_cuda):
+    """64 chains x 16384 sites, FP32 energy changes: incremental cf/energy vs the FP64 recompute after 3 sweeps."""
+    import torch
+    from cemc_gb300 import engine as E
+    from cemc_gb300.batch import fold_chemical_potential, sgc_grid
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(16, 4, 2, 1, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(0)
+    occ = rng.integers(0, 2, (64, m.n_sites)).astype(np.int8)
+    Ts, mus = sgc_grid()
+    ev = fold_chemical_potential(m, m.eci_vector(eci), mus)
+    cb = E.ChainBatch(geo, occ, ev, KB * Ts, E.MOVE_FLIP, seed=3)
+    cb.run(3 * m.n_sites, precision=E.PREC_F32, warps=24)
+    torch.cuda.synchronize()
+    cf_inc, e_inc = cb.cf.cpu().numpy().copy(), cb.energy.cpu().numpy().copy()
+    cb.recompute()
+    torch.cuda.synchronize()
+    cf_full, e_full = cb.cf.cpu().numpy(), cb.energy.cpu().numpy()
+    assert np.max(np.abs(cf_inc - cf_full)) < 1e-9  # binary products are exact in FP32
+    assert np.max(np.abs(e_inc - e_full)) < 1e-6
+    # singlet = mean spin (a size-independent identity)
+    spins = np.where(cb.occ.cpu().numpy() == 0, 1.0, -1.0).mean(axis=1)
+    assert np.allclose(cf_full[:, m.eci_names.index("c1_0")], spins, atol=1e-14)

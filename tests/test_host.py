@@ -75,7 +75,7 @@ def test_library_rejects_bad_descriptors_without_a_gpu():
     d.n_sites = 0
     assert L.cemc_geometry_create(ctypes.byref(d), ctypes.byref(handle)) == _lib.ERR_ARG
     assert L.cemc_run(None, None, None) == _lib.ERR_ARG
-    assert L.cemc_pt_exchange(0, 0, 0, 0, None, None, None, None, None) == _lib.ERR_ARG
+    assert L.cemc_pt_exchange(0, 0, 0, 0, None, None, None, None, None, None) == _lib.ERR_ARG
 
 
 def test_asymmetric_neighbour_table_is_rejected():
