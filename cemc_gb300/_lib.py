@@ -89,12 +89,14 @@ def load():
         L.cemc_recompute_scratch_doubles.argtypes = [_P, C.c_int32]
         L.cemc_recompute.argtypes = [_P, C.c_int32, _P, _P, _P, _P, _P, _P]
         L.cemc_energy.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
+        L.cemc_recompute_noalloc.argtypes = [_P, C.c_int32, _P, _P, _P, _P, _P]
         L.cemc_apply_changes.argtypes = [_P, _P, _P, _P, _P, C.c_int32, _P, _P, _P, _P, _P]
         L.cemc_delta_e.argtypes = [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]
         L.cemc_pt_exchange.argtypes = [C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, _P, _P, _P, _P, _P, _P]
         L.cemc_last_error.argtypes = [C.c_char_p, C.c_size_t]
         L.cemc_version.argtypes = [C.POINTER(C.c_int32)] * 3
         for name in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_run", "cemc_recompute", "cemc_energy",
+                     "cemc_recompute_noalloc",
                      "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error", "cemc_version"):
             getattr(L, name).restype = C.c_int
         _lib = L
@@ -113,7 +115,7 @@ def exported_symbols():
     L = load()
     names = []
     for n in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_run", "cemc_recompute_scratch_doubles",
-              "cemc_recompute", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
+              "cemc_recompute", "cemc_recompute_noalloc", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
               "cemc_version"):
         if hasattr(L, n):
             names.append(n)

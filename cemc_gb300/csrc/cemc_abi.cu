@@ -339,6 +339,28 @@ extern "C" int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const 
   return CEMC_OK;
 }
 
+extern "C" int cemc_recompute_noalloc(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ,
+                                      const double *eci, double *cf, double *energy, void *stream) {
+  if (!geo || n_chains <= 0 || !occ || !eci || !cf || !energy)
+    return fail(CEMC_ERR_ARG, "bad recompute_noalloc arguments");
+  if (n_chains > 65535) return fail(CEMC_ERR_LIMIT, "too many chains in one recompute");
+  const size_t need = cemc::recompute_blocks(geo->g) * (size_t)n_chains * (size_t)geo->g.n_eci;
+  if (need > cemc::kNoAllocScratchDoubles)
+    return fail(CEMC_ERR_LIMIT,
+                "recompute_noalloc needs %zu scratch doubles but its fixed array holds %zu "
+                "(reduce n_chains or call cemc_recompute with a caller buffer)",
+                need, cemc::kNoAllocScratchDoubles);
+  cudaError_t err = cudaSuccess;
+  double *scratch = cemc::noalloc_scratch(&err);
+  if (!scratch) return cuda_fail(err, "cudaGetSymbolAddress(recompute_noalloc scratch)");
+  // Each scratch entry the second kernel reads is written by the first kernel
+  // of the same call, so nothing has to be cleared between calls.
+  cudaError_t e = cemc::launch_recompute(geo->g, n_chains, occ, eci, cf, energy, scratch,
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "recompute_noalloc kernel launch");
+  return CEMC_OK;
+}
+
 extern "C" int cemc_energy(const cemc_geometry *geo, int32_t n_chains, const double *eci, const double *cf,
                            double *energy, void *stream) {
   if (!geo || n_chains <= 0 || !eci || !cf || !energy) return fail(CEMC_ERR_ARG, "bad energy arguments");

@@ -5,10 +5,42 @@
 //   * replica exchange over a temperature ladder.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "cemc_device.cuh"
 #include "cemc_kernels.h"
 
 namespace cemc {
+
+// Scratch of cemc_recompute_noalloc: the per-block partial sums of the full
+// recompute live in this fixed device array instead of a caller buffer, so
+// that entry point allocates nothing.  Every GPU that loads the library holds
+// it (8 MiB) until the process exits.  Host code must not use the symbol as a
+// pointer: noalloc_scratch() resolves its device address per device.
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+double *noalloc_scratch(cudaError_t *err) {
+  static std::mutex mu;
+  static std::unordered_map<int, double *> addr;  // device ordinal -> address of g_noalloc_scratch there
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *err = e;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = addr.find(dev);
+  if (it != addr.end()) return it->second;
+  double *p = nullptr;
+  e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
+  if (e != cudaSuccess) {
+    *err = e;
+    return nullptr;
+  }
+  addr[dev] = p;
+  return p;
+}
 
 // ---------------------------------------------------------------------------
 // Full recompute.  Block (bx, chain) handles sites [bx*256, bx*256+256) of one

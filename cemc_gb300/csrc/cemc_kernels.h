@@ -6,6 +6,11 @@
 
 namespace cemc {
 
+// Capacity (doubles) of the fixed scratch array behind cemc_recompute_noalloc.
+constexpr size_t kNoAllocScratchDoubles = (size_t)1 << 20;
+// Device address of that array on the current device (resolved once per device).
+double *noalloc_scratch(cudaError_t *err);
+
 size_t recompute_blocks(const DevGeo &g);
 size_t warp_kernel_smem(const DevGeo &g);
 cudaError_t launch_recompute(const DevGeo &g, int n_chains, const int8_t *occ, const double *eci, double *cf,

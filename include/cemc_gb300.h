@@ -150,6 +150,25 @@ size_t cemc_recompute_scratch_doubles(const cemc_geometry *geo, int32_t n_chains
 int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
                    double *cf, double *energy, double *scratch, void *stream);
 
+/* Full recompute that allocates nothing (no reference counterpart: the
+ * reference computes correlation functions on the host).  Same results as
+ * cemc_recompute(), but its scratch is a fixed array inside the library
+ * instead of a caller buffer, for callers that cannot allocate device memory
+ * when they call it -- for example a process that has already handed its
+ * whole device-memory budget to a pre-reserved pool, or a latency-critical
+ * path where cudaMalloc's implicit device synchronisation is not acceptable.
+ * Limit: recompute_blocks * n_chains * n_eci <= 1048576 scratch doubles
+ * (8 MiB, held on every GPU that loads the library until exit); larger
+ * requests return CEMC_ERR_LIMIT without launching anything, where
+ * recompute_blocks = ceil(n_sites / 256).  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU (other streams, other threads) race: order
+ * them on one stream or synchronise between them.  It never calls cudaMalloc,
+ * cudaFree or an allocating library routine. */
+int cemc_recompute_noalloc(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
+                           double *cf, double *energy, void *stream);
+
 /* Energy N * sum_k eci[k] * cf[k] of every chain, summed in sorted-name order
  * (CEUpdater::get_energy + NamedArray::dot, ce_updater.cpp:236-242,
  * named_array.cpp:25-33).  Device pointers. */
