@@ -200,6 +200,65 @@ def calibrated_cpu_sample(m, occ, ev, Ts, threads: int, target_s: float):
     return sweeps
 
 
+def correctness_sample(geo, m, occ, ev, Ts, n_trials: int = 40000, chain: int = N_CHAINS - 1):
+    """FP32 energy changes vs the FP64 oracle on one chain of the workload (the hottest, highest-acceptance one)."""
+    import torch
+    from cemc_gb300 import engine as E
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    kT = KB * Ts[chain]
+    cb = E.ChainBatch(geo, occ[chain:chain + 1], ev[chain:chain + 1], kT, E.MOVE_FLIP, seed=77)
+    _, acc, de = cb.run(n_trials, precision=E.PREC_F32, warps=8, trace=True)
+    torch.cuda.synchronize()
+    acc, de = acc.cpu().numpy()[0], de.cpu().numpy()[0]
+    orc = O.Oracle(m)
+    st = orc.new_chain_state(occ[chain], ev[chain], kT, O.MOVE_FLIP)
+    tr = orc.run(st, seed=77, chain_id=0, t_begin=0, n_trials=n_trials, trace=True)
+    band = 1e-5 / kT
+    margin = np.abs(tr.de / kT + np.log(np.maximum(tr.u, 1e-300)))
+    mism = acc != tr.acc
+    first = int(np.argmax(mism)) if mism.any() else n_trials
+    same = slice(0, first)
+    return {"chain": chain, "T": float(Ts[chain]), "trials": n_trials, "accept_rate": float(tr.acc.mean()),
+            "max_abs_dE_error_eV": float(np.max(np.abs(de[same] - tr.de[same]))) if first else 0.0,
+            "decision_mismatches": int(mism.sum()), "near_threshold_trials": int((margin < band).sum()),
+            "band": "|dE/kT + ln u| < 1e-5 eV / kT",
+            "final_energy_rel_error": float(abs(cb.energy.item() - st.energy[0]) / abs(st.energy[0]))
+            if not mism.any() else None}
+
+
+def run_served(args):
+    """Served stream: Poisson arrivals of mixed jobs through the continuous-batching server."""
+    import torch
+    from cemc_gb300.server import MCServer, poisson_stream
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    jobs = poisson_stream(args.served_jobs, rate=200.0, seed=rank,
+                          sweeps_range=(1e2 * args.served_sweep_scale, 1e4 * args.served_sweep_scale))
+    srv = MCServer(quantum_sweeps=10.0, capacity=64, hbm_budget_gb=120.0)
+    t0 = time.perf_counter()
+    i = 0
+    while i < len(jobs) or srv.pending or any(g.active() for g in srv.groups.values()):
+        now = time.perf_counter() - t0
+        while i < len(jobs) and jobs[i].arrival <= now:
+            jobs[i].arrival = t0 + jobs[i].arrival
+            srv.submit(jobs[i])
+            i += 1
+        srv.step()
+    st = srv.stats()
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload": "served_stream", "value": st["trials_per_s"], "unit": UNIT,
+                          "p50_latency_s": st["p50_latency_s"], "p99_latency_s": st["p99_latency_s"],
+                          "jobs": st["jobs"], "wall_s": st["wall_s"], "hbm_used_gb": st["hbm_used_gb"],
+                          "config": {"arrivals": "Poisson 200 jobs/s", "n_jobs": args.served_jobs,
+                                     "supercells": "4^3-32^3 conventional, log-uniform",
+                                     "sweeps": "%g-%g log-uniform" % (1e2 * args.served_sweep_scale,
+                                                                     1e4 * args.served_sweep_scale),
+                                     "recipes": "binary, binary to 6th shell, ternary; SGC and canonical",
+                                     "T": "U[300,1200] K", "hbm_budget_gb": 120}}))
+    return 0
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -344,6 +403,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         plain = n_launch * m.n_sites / (time.perf_counter() - t0)
 
+    corr = correctness_sample(geo, m, occ, ev, Ts) if rank == 0 and not args.no_correctness else None
+
     # -- CPU baseline on a bounded sample (rank 0) --------------------------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -375,6 +436,7 @@ def run_gpu(args):
             "plain_gpu": {"value": plain, "unit": UNIT,
                           "form": "one chain per launch, FP64 energy change, one sweep per launch, no graph"},
             "cpu_baseline": cpu,
+            "correctness": corr,
             "thermo_sample": {"chain0": thermo[0], "chain63": thermo[-1]},
         }
         print(json.dumps(line))
@@ -394,6 +456,12 @@ def main(argv=None):
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)
+    p.add_argument("--no-correctness", action="store_true")
+    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served"],
+                   help="sgc64: the headline 64-chain batch; served: the Poisson job stream")
+    p.add_argument("--served-jobs", type=int, default=300)
+    p.add_argument("--served-sweep-scale", type=float, default=0.1,
+                   help="scale of the served jobs' sweep budgets (1 = 10^2-10^4 sweeps)")
     p.add_argument("--profile", action="store_true",
                    help="profiling case: the timed steps only (no end-to-end, plain-GPU or CPU legs)")
     args = p.parse_args(argv)
@@ -401,6 +469,8 @@ def main(argv=None):
         p.error("at least 3 warm-up steps")
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_gpu(args)
 
 

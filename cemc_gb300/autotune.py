@@ -18,7 +18,7 @@ import torch
 
 from . import engine as E
 
-CANDIDATES = (4, 8, 12, 16, 24, 32)
+CANDIDATES = (1, 2, 4, 8, 12, 16, 24, 31)
 _CACHE_PATH = os.environ.get("CEMC_AUTOTUNE_CACHE",
                              os.path.join(os.path.expanduser("~"), ".cache", "cemc_gb300", "autotune.json"))
 _lock = threading.Lock()
@@ -77,7 +77,30 @@ def tune(geo, move: int, precision: int, n_chains: int, candidates: Sequence[int
     return out
 
 
-def best_warps(geo, move: int, precision: int, n_chains: int) -> int:
+def tune_on(cb, precision: int, candidates: Sequence[int] = CANDIDATES, sweeps: float = 0.25) -> Dict[int, float]:
+    """Trials/s of each width on the caller's own batch; its state is restored afterwards."""
+    names = ["occ", "cf", "energy", "trial", "accum"] + (["trk", "loc"] if cb.trk is not None else [])
+    snap = {n: getattr(cb, n).clone() for n in names}
+    trials = max(256, int(sweeps * cb.geo.n_sites))
+    stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
+    out = {}
+    for w in candidates:
+        cb.run(trials // 4, precision=precision, warps=w)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)  # the kernel runs on the batch's stream
+        cb.run(trials, precision=precision, warps=w)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[int(w)] = cb.n_chains * trials / (e0.elapsed_time(e1) * 1e-3)
+        for n, t in snap.items():
+            getattr(cb, n).copy_(t)
+    torch.cuda.synchronize()
+    return out
+
+
+def best_warps(geo, move: int, precision: int, n_chains: int, batch=None) -> int:
+    """Cached best width for this geometry/move/precision/chain count; tuned on ``batch`` when given."""
     key = _key(geo, move, precision, n_chains)
     with _lock:
         if key in _mem:
@@ -86,7 +109,7 @@ def best_warps(geo, move: int, precision: int, n_chains: int) -> int:
         if key in disk:
             _mem[key] = int(disk[key])
             return _mem[key]
-    rates = tune(geo, move, precision, n_chains)
+    rates = tune_on(batch, precision) if batch is not None else tune(geo, move, precision, n_chains)
     best = max(rates, key=rates.get)
     with _lock:
         _mem[key] = best

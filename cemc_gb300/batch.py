@@ -38,7 +38,7 @@ class BatchRunner:
         self.precision = int(precision)
         if warps == 0:
             from .autotune import best_warps
-            warps = best_warps(geo, move, self.precision, self.cb.n_chains)
+            warps = best_warps(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
         self.warps = int(warps)
         self.trials_per_step = max(1, int(round(sweeps_per_step * geo.n_sites)))
         self.recompute_every = max(0, int(recompute_every))

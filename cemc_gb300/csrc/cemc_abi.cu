@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "cemc_kernels.h"
+#include "cemc_spin.h"
 
 namespace {
 
@@ -39,6 +40,8 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct cemc_geometry {
   cemc::DevGeo g;
+  cemc::SpinDev spin{};  // tables of the binary spin-basis kernel (spin_ok)
+  bool spin_ok = false;
   void *dev = nullptr;  // one device allocation holding every table
   int max_smem = 0;     // opt-in shared memory per block of the current device
 };
@@ -167,6 +170,67 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
     for (int c = 0; c < C; ++c) table_cm[(size_t)c * N + i] = d->table[(size_t)i * C + c];
   std::vector<double> w(d->eci_weight, d->eci_weight + K), fw(d->eci_full_weight, d->eci_full_weight + K);
 
+  // Binary spin basis (values +1 / -1): pair terms of a cluster ECI folded into
+  // one shell mask; the other terms sorted by ECI and cut into 32 lane ranges.
+  std::vector<cemc::SpinEci> spin_eci;
+  std::vector<uint32_t> spin_masks;  // (lo, hi) pairs
+  std::vector<int> spin_mask_cl;     // cluster-ECI slot of each mask
+  std::vector<uint8_t> spin_shift;
+  std::vector<int32_t> spin_lane_term(33, 0), spin_lane_first(32, 0);
+  int minus_id = -1, singlet_eci = -1;
+  bool spin_ok = (B == 1 && S == 2 && C <= CEMC_SPIN_MAX_COLS);
+  if (spin_ok) {
+    if (d->bf[0] == 1.0 && d->bf[1] == -1.0)
+      minus_id = 1;
+    else if (d->bf[0] == -1.0 && d->bf[1] == 1.0)
+      minus_id = 0;
+    else
+      spin_ok = false;
+  }
+  for (int k = 0; spin_ok && k < K; ++k) {
+    if (d->eci_kind[k] == 1) singlet_eci = k;
+    if (d->eci_kind[k] != 2) continue;
+    cemc::SpinEci e{};
+    e.eci = k;
+    uint64_t pairs = 0;
+    for (int t = fterm_off[k]; t < fterm_off[k + 1]; ++t) {
+      uint64_t m = 0;
+      for (int j = 0; j < d->term_size[t] - 1; ++j) m |= (uint64_t)1 << (d->term_nb[3 * t + j]);
+      if (d->term_size[t] == 2 && !(pairs & m)) {
+        pairs |= m;
+        e.n_pairs++;
+      } else {
+        spin_masks.push_back((uint32_t)m);
+        spin_masks.push_back((uint32_t)(m >> 32));
+        spin_mask_cl.push_back((int)spin_eci.size());
+        e.n_multi++;
+      }
+    }
+    e.pair_lo = (uint32_t)pairs;
+    e.pair_hi = (uint32_t)(pairs >> 32);
+    spin_eci.push_back(e);
+  }
+  if (spin_ok && (spin_eci.empty() || spin_eci.size() > CEMC_SPIN_MAX_CL)) spin_ok = false;
+  const int n_masks = (int)spin_mask_cl.size();
+  if (spin_ok) {
+    const int q = (n_masks + 31) / 32;
+    for (int l = 0; l <= 32; ++l) spin_lane_term[l] = std::min(l * q, n_masks);
+    spin_shift.assign(std::max(n_masks, 1), 0);
+    for (int l = 0; l < 32 && spin_ok; ++l) {
+      const int lo = spin_lane_term[l], hi = spin_lane_term[l + 1];
+      if (lo >= hi) continue;
+      spin_lane_first[l] = spin_mask_cl[lo];
+      for (int t = lo; t < hi; ++t) {
+        const int sl = spin_mask_cl[t] - spin_lane_first[l];
+        if (sl > 4 || hi - lo > 63) spin_ok = false;  // 5 six-bit counters per lane
+        spin_shift[t] = (uint8_t)(6 * sl);
+      }
+    }
+  }
+  if (spin_eci.empty()) spin_eci.push_back(cemc::SpinEci{});
+  if (spin_masks.empty()) spin_masks.assign(2, 0u);
+  if (spin_shift.empty()) spin_shift.assign(1, 0);
+
   // One device allocation for all tables.
   struct Part {
     const void *src;
@@ -181,6 +245,11 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {w.data(), sizeof(double) * K, 0},           {fw.data(), sizeof(double) * K, 0},
       {d->bf, sizeof(double) * B * S, 0},          {fterms.data(), fterms.size(), 0},
       {fterm_off.data(), fterm_off.size() * 4, 0},
+      {spin_eci.data(), spin_eci.size() * sizeof(cemc::SpinEci), 0},
+      {spin_masks.data(), spin_masks.size() * 4, 0},
+      {spin_shift.data(), spin_shift.size(), 0},
+      {spin_lane_term.data(), 33 * 4, 0},
+      {spin_lane_first.data(), 32 * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -227,6 +296,16 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.fterms = reinterpret_cast<const uint8_t *>(base + parts[11].off);
   g.fterm_off = reinterpret_cast<const int32_t *>(base + parts[12].off);
   for (int b = 0; b < CEMC_MAX_BF; ++b) g.singlet_eci[b] = singlet[b];
+  geo->spin_ok = spin_ok;
+  geo->spin.n_cl = spin_ok ? (int)spin_eci.size() : 0;
+  geo->spin.n_masks = spin_ok ? n_masks : 0;
+  geo->spin.minus_id = minus_id;
+  geo->spin.singlet_eci = singlet_eci;
+  geo->spin.eci = reinterpret_cast<const cemc::SpinEci *>(base + parts[13].off);
+  geo->spin.masks = reinterpret_cast<const uint2 *>(base + parts[14].off);
+  geo->spin.shift = reinterpret_cast<const uint8_t *>(base + parts[15].off);
+  geo->spin.lane_term = reinterpret_cast<const int32_t *>(base + parts[16].off);
+  geo->spin.lane_first = reinterpret_cast<const int32_t *>(base + parts[17].off);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&geo->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -281,6 +360,10 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   a.chain_key = r->chain_key;
   a.accum_slot = r->accum_slot;
   a.chain_trials = r->chain_trials;
+  const bool use_spin = (r->kernel == CEMC_KERNEL_SPIN) || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
+  if (r->kernel == CEMC_KERNEL_SPIN && !geo->spin_ok)
+    return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
+  const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
   // Shared memory: the occupation, then (swaps) the site lists, then an exact
   // stamp table (one entry per site) are preferred; fall back in that order.
   const size_t budget = (size_t)geo->max_smem;
@@ -296,7 +379,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   cemc::McLayout L{};
   for (const Choice &ch : choices) {
     for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
-      L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits);
+      L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks);
       if (L.total <= budget) {
         a.occ_smem = ch.occ;
         a.trk_smem = ch.trk;
@@ -316,7 +399,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     const uint64_t n = std::min(max_chunk, r->n_trials - done);
     a.n_trials = n;
     a.chunk_offset = done;
-    cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream));
+    cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream),
+                                    use_spin ? &geo->spin : nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "Monte Carlo kernel launch");
     done += n;
   }

@@ -67,6 +67,47 @@ __device__ __forceinline__ R warp_scan_incl(R v, int lane) {
   return v;
 }
 
+// Double-float: a value carried as an unevaluated sum hi + lo of two floats
+// (about 48 significant bits), added and multiplied on the FP32 pipe with the
+// error-free transformations TwoSum (Knuth) and TwoProd (by fused multiply-add).
+// The Monte Carlo kernel keeps its per-round running sums in this form in FP32
+// mode: FP64 instructions are slow to issue on this part and would otherwise
+// sit on the critical path of every round.  Values move to FP64 once per launch.
+struct df64 {
+  float hi, lo;
+};
+__device__ __forceinline__ df64 df_from(double d) {
+  df64 r;
+  r.hi = (float)d;
+  r.lo = (float)(d - (double)r.hi);
+  return r;
+}
+__device__ __forceinline__ double df_to(df64 a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ df64 df_norm(float s, float e) {
+  const float hi = __fadd_rn(s, e);
+  df64 r;
+  r.hi = hi;
+  r.lo = __fsub_rn(e, __fsub_rn(hi, s));
+  return r;
+}
+__device__ __forceinline__ df64 df_add(df64 a, float b) {
+  const float s = __fadd_rn(a.hi, b);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return df_norm(s, __fadd_rn(a.lo, e));
+}
+__device__ __forceinline__ df64 df_add(df64 a, df64 b) { return df_add(df_add(a, b.hi), b.lo); }
+__device__ __forceinline__ df64 df_mul(df64 a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  const float e = __fmaf_rn(a.hi, b, -p);
+  return df_norm(p, __fmaf_rn(a.lo, b, e));
+}
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return df_norm(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+
 // Metropolis test of the reference, accept = (dE < 0) or (u <= exp(-dE / kT))
 // (cemc/mcmc/montecarlo.py:950-956), with u the 53-bit uniform of words (a, b).
 // The test is first made in single precision as ln(u) + dE/kT against a

@@ -42,6 +42,7 @@ struct Draw {
 
 struct McLayout {
   size_t cf, eci, w, acc, coef, bf, terms, lane_term, kind, misc;
+  size_t sp_eci, sp_masks, sp_shift, sp_lane;  // spin-basis tables (empty unless n_cl > 0)
   size_t rec, rec_stride, rec_tsa, rec_tsb, rec_acc, rec_der, rec_de, rec_d;
   size_t draws, rows;
   size_t warp0, warp_stride, warp_part;
@@ -54,7 +55,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 
 // Shared-memory carve-up of mc_kernel for `warps` evaluating warps.
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
-                                              int trk_smem, int stamp_bits) {
+                                              int trk_smem, int stamp_bits, int n_cl = 0, int n_masks = 0) {
   McLayout L;
   size_t o = 0;
   const size_t K = (size_t)g.n_eci;
@@ -64,8 +65,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 8 * K);
   L.w = o;
   o = align16(o + 8 * K);
-  L.acc = o;
-  o = align16(o + 8 * (size_t)(2 + 3 * CEMC_MAX_BF));
+  L.acc = o;  // running sums (14), singlets at launch start (4), 1/N, then per-ECI launch deltas (n_eci)
+  o = align16(o + 8 * (size_t)(2 + 3 * CEMC_MAX_BF + CEMC_MAX_BF + 1 + K));
   L.coef = o;
   o = align16(o + (size_t)rsize * K);
   L.bf = o;
@@ -78,6 +79,14 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 2 * K);
   L.misc = o;
   o = align16(o + 4 * 64);
+  L.sp_eci = o;
+  o = align16(o + 32 * (size_t)n_cl);
+  L.sp_masks = o;
+  o = align16(o + 8 * (size_t)n_masks);
+  L.sp_shift = o;
+  o = align16(o + (size_t)n_masks);
+  L.sp_lane = o;
+  if (n_cl > 0) o = align16(o + 4 * (33 + 32));
   // two buffers of per-trial records (current round / round being booked)
   L.rec_tsa = 0;
   L.rec_tsb = 4 * 32;
@@ -108,6 +117,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   return L;
 }
 
-cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st);
+struct SpinDev;
+cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
+                      const SpinDev *spin);
 
 }  // namespace cemc

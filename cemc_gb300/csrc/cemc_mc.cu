@@ -34,6 +34,7 @@
 
 #include "cemc_device.cuh"
 #include "cemc_launch.h"
+#include "cemc_spin.h"
 
 namespace cemc {
 
@@ -66,12 +67,53 @@ __device__ __forceinline__ void gather_smem_row(const DevGeo &g, const int8_t *o
   }
 }
 
-template <typename R, int MOVE>
-__global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
+// Spin word of a neighbour row (binary +1/-1 basis): bit c = 1 when column c
+// holds the -1 species; one ballot per 32 columns.  `ovr_site` reads as spin
+// bit `ovr_bit` (the first half of a swap already applied).
+__device__ __forceinline__ void spin_ballot(const DevGeo &g, const int8_t *occ, const int32_t *row, uint32_t xorv,
+                                            int ovr_site, uint32_t ovr_bit, uint32_t &lo, uint32_t &hi,
+                                            int (&nbr)[4], int lane) {
+  uint32_t b0 = 0, b1 = 0;
+  nbr[0] = nbr[1] = nbr[2] = nbr[3] = -1;
+  if (lane < g.n_cols) {
+    const int s = row[lane];
+    nbr[0] = s;
+    b0 = (s == ovr_site) ? ovr_bit : ((uint32_t)occ[s] ^ xorv);
+  }
+  if (lane + 32 < g.n_cols) {
+    const int s = row[lane + 32];
+    nbr[1] = s;
+    b1 = (s == ovr_site) ? ovr_bit : ((uint32_t)occ[s] ^ xorv);
+  }
+  lo = __ballot_sync(kFull, b0);
+  hi = __ballot_sync(kFull, b1);
+}
+
+// Parities of this lane's multi-site terms, packed 6 bits per cluster-ECI slot.
+__device__ __forceinline__ uint32_t spin_lane_parities(const uint2 *masks, const uint8_t *shift, int lo_t, int hi_t,
+                                                       uint32_t lo, uint32_t hi) {
+  uint32_t packed = 0;
+  for (int t = lo_t; t < hi_t; ++t) {
+    const uint2 m = masks[t];
+    packed += (uint32_t)(__popc((lo & m.x) ^ (hi & m.y)) & 1) << shift[t];
+  }
+  return packed;
+}
+
+// Number of odd-parity multi-site terms of cluster ECI k over the warp.
+__device__ __forceinline__ int spin_odd(uint32_t packed, int k, int first) {
+  const int sl = k - first;
+  const int v = (sl >= 0 && sl < 5) ? (int)((packed >> (6 * sl)) & 63u) : 0;
+  return __reduce_add_sync(kFull, v);
+}
+
+template <typename R, int MOVE, bool SPIN>
+__global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
   const int W = a.warps;  // evaluating warps; warp W is the helper
-  const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits);
+  const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits, SPIN ? sd.n_cl : 0,
+                               SPIN ? sd.n_masks : 0);
   const int chain = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool helper = (warp == W);
@@ -81,7 +123,13 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   double *cf_s = reinterpret_cast<double *>(smem + L.cf);
   double *eci_s = reinterpret_cast<double *>(smem + L.eci);
   double *w_s = reinterpret_cast<double *>(smem + L.w);
-  double *acc_s = reinterpret_cast<double *>(smem + L.acc);  // 2 + 3 * CEMC_MAX_BF running sums of this launch
+  // Running sums of this launch: FP64 in FP64 mode; double-float in FP32 mode, where
+  // the correlation functions also accumulate per-launch deltas (applied in the epilogue).
+  constexpr bool DF = (sizeof(R) == 4);
+  constexpr int NACC = 2 + 3 * CEMC_MAX_BF;
+  double *acc_s = reinterpret_cast<double *>(smem + L.acc);
+  df64 *accd = reinterpret_cast<df64 *>(smem + L.acc);      // [NACC] sums, [NACC..+4) singlet starts, [NACC+4] 1/N
+  df64 *dcf = accd + NACC + CEMC_MAX_BF + 1;                // [n_eci] launch deltas (FP32 mode)
   R *coef_s = reinterpret_cast<R *>(smem + L.coef);
   R *bf_s = reinterpret_cast<R *>(smem + L.bf);
   uint16_t *terms_s = reinterpret_cast<uint16_t *>(smem + L.terms);
@@ -102,6 +150,13 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   R *vb = va + g.vals_len;
   R *part = reinterpret_cast<R *>(wbase + L.warp_part);
 
+  SpinEci *sp_eci = reinterpret_cast<SpinEci *>(smem + L.sp_eci);
+  uint2 *sp_masks = reinterpret_cast<uint2 *>(smem + L.sp_masks);
+  uint8_t *sp_shift = reinterpret_cast<uint8_t *>(smem + L.sp_shift);
+  int32_t *sp_lane_term = reinterpret_cast<int32_t *>(smem + L.sp_lane);
+  int32_t *sp_lane_first = sp_lane_term + 33;
+  const uint32_t xorv = SPIN ? (uint32_t)(sd.minus_id ^ 1) : 0u;  // spin bit = occ ^ xorv (1 = the -1 species)
+
   int8_t *occ = a.occ_smem ? reinterpret_cast<int8_t *>(smem + L.occ) : a.occ + (size_t)chain * N;
   int32_t *trk = nullptr, *loc = nullptr;
   if (SWAP) {
@@ -113,6 +168,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   for (int k = tid; k < n_eci; k += blockDim.x) {
     const int kind = g.eci_kind[k];
     const double e = a.eci[(size_t)chain * n_eci + k];
+    if (DF) dcf[k] = df64{0.f, 0.f};
     cf_s[k] = a.cf[(size_t)chain * n_eci + k];
     eci_s[k] = e;
     w_s[k] = (kind == 2) ? g.eci_w[k] : 0.0;
@@ -131,6 +187,15 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
   for (uint32_t i = tid; i <= hmask; i += blockDim.x) stamp[i] = 0u;
+  if (SPIN) {
+    for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
+    for (int t = tid; t < sd.n_masks; t += blockDim.x) {
+      sp_masks[t] = sd.masks[t];
+      sp_shift[t] = sd.shift[t];
+    }
+    for (int i = tid; i < 33; i += blockDim.x) sp_lane_term[i] = sd.lane_term[i];
+    for (int i = tid; i < 32; i += blockDim.x) sp_lane_first[i] = sd.lane_first[i];
+  }
   if (a.occ_smem) {
     const int8_t *src = a.occ + (size_t)chain * N;
     for (int i = tid; i < N; i += blockDim.x) occ[i] = src[i];
@@ -155,7 +220,14 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
       misc[2] = np;
       if (np < 2) misc[1] = CEMC_ERR_STATE;
     }
-    for (int i = 0; i < 2 + 3 * CEMC_MAX_BF; ++i) acc_s[i] = 0.0;
+    if (DF) {
+      for (int i = 0; i < NACC; ++i) accd[i] = df64{0.f, 0.f};
+      for (int b = 0; b < CEMC_MAX_BF; ++b)
+        accd[NACC + b] = b < g.n_bf ? df_from(a.cf[(size_t)chain * n_eci + g.singlet_eci[b]]) : df64{0.f, 0.f};
+      accd[NACC + CEMC_MAX_BF] = df_from(1.0 / (double)N);
+    } else {
+      for (int i = 0; i < NACC; ++i) acc_s[i] = 0.0;
+    }
   }
 
   const double kT = a.kT[chain];
@@ -173,7 +245,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   const double e_ref = a.accum ? a.accum[acc_row].e_ref : 0.0;
 
   // Helper-warp state.
-  double energy = a.energy[chain];
+  double energy = a.energy[chain];                               // FP64 mode: E
+  df64 eoff = DF ? df_from(a.energy[chain] - e_ref) : df64{0.f, 0.f};  // FP32 mode: E - e_ref
   uint64_t n_acc_launch = 0;
   uint64_t fill_end = t_first;
 
@@ -209,6 +282,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   };
 
   // Fold round records (buffer `rec`, `ks` committed trials) into the FP64 state.
+  // Lanes are trials; every per-round total is a warp reduction, several
+  // interleaved, and the FP64 folds are independent of each other.
   auto book = [&](const unsigned char *rec, int ks) {
     const int8_t *tacc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
     const R *tder = reinterpret_cast<const R *>(rec + L.rec_der);
@@ -216,42 +291,110 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     const bool mine = lane < ks;
     const bool acc = mine && tacc[lane];
     n_acc_launch += (uint64_t)__popc(__ballot_sync(kFull, acc));
-    const R X = warp_scan_incl<R>(acc ? tder[lane] : (R)0, lane);  // energy offset after trial `lane`
-    const R x_tot = __shfl_sync(kFull, X, ks - 1);
-    if (a.accum) {
-      const R sX = warp_sum(mine ? X : (R)0);
-      const R sX2 = warp_sum(mine ? X * X : (R)0);
-      const double ea = energy - e_ref;
-      if (lane == 0) {
-        acc_s[0] += (double)ks * ea + (double)sX;
-        acc_s[1] += (double)ks * ea * ea + 2.0 * ea * (double)sX + (double)sX2;
+    const R *Dl = tD + (size_t)lane * n_eci;
+    constexpr int NS = 1 + CEMC_MAX_BF;  // energy offset and singlet offsets, scanned together
+    R sc[NS];
+    sc[0] = acc ? tder[lane] : (R)0;
+#pragma unroll
+    for (int b = 0; b < CEMC_MAX_BF; ++b) sc[1 + b] = (acc && b < g.n_bf) ? Dl[g.singlet_eci[b]] : (R)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        const R n = __shfl_up_sync(kFull, sc[q], o);
+        if (lane >= o) sc[q] += n;
       }
-      for (int b = 0; b < g.n_bf; ++b) {
-        const int kb = g.singlet_eci[b];
-        const R DS = warp_scan_incl<R>(acc ? tD[lane * n_eci + kb] : (R)0, lane);  // N * singlet offset
-        const R sD = warp_sum(mine ? DS : (R)0);
-        const R sD2 = warp_sum(mine ? DS * DS : (R)0);
-        const R sDX = warp_sum(mine ? DS * X : (R)0);
-        if (lane == 0) {
-          const double s0 = cf_s[kb], inv_n = 1.0 / (double)N;
-          acc_s[2 + b] += (double)ks * s0 + (double)sD * inv_n;
-          acc_s[2 + CEMC_MAX_BF + b] += (double)ks * s0 * s0 + 2.0 * s0 * (double)sD * inv_n +
-                                        (double)sD2 * inv_n * inv_n;
-          acc_s[2 + 2 * CEMC_MAX_BF + b] += (double)ks * s0 * ea + s0 * (double)sX + ea * (double)sD * inv_n +
-                                            (double)sDX * inv_n;
+    }
+    const R x_tot = __shfl_sync(kFull, sc[0], ks - 1);
+    if (a.accum) {
+      // sums over the round of X, X^2 and, per singlet, DS, DS^2, DS*X (X, DS: offsets after each trial)
+      constexpr int NR = 2 + 3 * CEMC_MAX_BF;
+      R r[NR];
+      const R X = sc[0];
+      r[0] = mine ? X : (R)0;
+      r[1] = mine ? X * X : (R)0;
+#pragma unroll
+      for (int b = 0; b < CEMC_MAX_BF; ++b) {
+        const R DS = sc[1 + b];
+        r[2 + 3 * b] = mine ? DS : (R)0;
+        r[3 + 3 * b] = mine ? DS * DS : (R)0;
+        r[4 + 3 * b] = mine ? DS * X : (R)0;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < NR; ++q) r[q] += __shfl_xor_sync(kFull, r[q], o);
+      }
+      if (lane == 0) {
+        if constexpr (DF) {
+          const float k = (float)ks, sX = (float)r[0], sX2 = (float)r[1];
+          const df64 ea = eoff, inv_n = accd[NACC + CEMC_MAX_BF];
+          accd[0] = df_add(df_add(accd[0], df_mul(ea, k)), sX);
+          accd[1] = df_add(df_add(df_add(accd[1], df_mul(df_mul(ea, ea), k)), df_mul(ea, 2.0f * sX)), sX2);
+#pragma unroll
+          for (int b = 0; b < CEMC_MAX_BF; ++b) {
+            if (b < g.n_bf) {
+              const df64 s0 = df_add(accd[NACC + b], df_mul(dcf[g.singlet_eci[b]], inv_n));
+              const df64 sD = df_mul(inv_n, (float)r[2 + 3 * b]);
+              const df64 sD2 = df_mul(df_mul(inv_n, inv_n), (float)r[3 + 3 * b]);
+              const df64 sDX = df_mul(inv_n, (float)r[4 + 3 * b]);
+              accd[2 + b] = df_add(df_add(accd[2 + b], df_mul(s0, k)), sD);
+              accd[2 + CEMC_MAX_BF + b] =
+                  df_add(df_add(df_add(accd[2 + CEMC_MAX_BF + b], df_mul(df_mul(s0, s0), k)), df_mul(df_mul(s0, sD), 2.0f)),
+                         sD2);
+              accd[2 + 2 * CEMC_MAX_BF + b] = df_add(
+                  df_add(df_add(df_add(accd[2 + 2 * CEMC_MAX_BF + b], df_mul(df_mul(s0, ea), k)), df_mul(s0, sX)),
+                         df_mul(ea, sD)),
+                  sDX);
+            }
+          }
+        } else {
+          const double ea = energy - e_ref, k = (double)ks, sX = (double)r[0], sX2 = (double)r[1];
+          const double inv_n = 1.0 / (double)N;
+          acc_s[0] += k * ea + sX;
+          acc_s[1] += k * ea * ea + 2.0 * ea * sX + sX2;
+#pragma unroll
+          for (int b = 0; b < CEMC_MAX_BF; ++b) {
+            if (b < g.n_bf) {
+              const double s0 = cf_s[g.singlet_eci[b]], sD = (double)r[2 + 3 * b] * inv_n;
+              const double sD2 = (double)r[3 + 3 * b] * inv_n * inv_n, sDX = (double)r[4 + 3 * b] * inv_n;
+              acc_s[2 + b] += k * s0 + sD;
+              acc_s[2 + CEMC_MAX_BF + b] += k * s0 * s0 + 2.0 * s0 * sD + sD2;
+              acc_s[2 + 2 * CEMC_MAX_BF + b] += k * s0 * ea + s0 * sX + ea * sD + sDX;
+            }
+          }
         }
       }
     }
     __syncwarp();
-    for (int k = lane; k < n_eci; k += 32) {
-      const int kind = kind_s[k];
-      if (kind == 0) continue;
-      R dsum = (R)0;
-      for (int j = 0; j < ks; ++j)
-        if (tacc[j]) dsum += tD[j * n_eci + k];
-      cf_s[k] = (kind == 2) ? cf_s[k] + (double)dsum * w_s[k] : cf_s[k] + (double)dsum / (double)N;
+    // correlation functions: per-ECI totals of the round's committed accepted changes
+    for (int k0 = 0; k0 < n_eci; k0 += 4) {
+      R v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = (acc && k0 + q < n_eci) ? Dl[k0 + q] : (R)0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], o);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = k0 + q;
+        if (lane == q && k < n_eci) {
+          if constexpr (DF) {
+            dcf[k] = df_add(dcf[k], (float)v[q]);
+          } else {
+            const int kind = kind_s[k];
+            if (kind == 2) cf_s[k] = cf_s[k] + (double)v[q] * w_s[k];
+            else if (kind == 1) cf_s[k] = cf_s[k] + (double)v[q] / (double)N;
+          }
+        }
+      }
     }
-    energy += (double)x_tot;
+    if constexpr (DF)
+      eoff = df_add(eoff, (float)x_tot);
+    else
+      energy += (double)x_tot;
     __syncwarp();
   };
 
@@ -286,6 +429,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
         int sa, sb = -1, na;
         int nbra[4], nbrb[4] = {-1, -1, -1, -1};
         uint32_t ua, ub;
+        uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
         if (!SWAP) {
           sa = dr.site;
           const int oa = occ[sa];
@@ -293,7 +437,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
           na = k + (k >= oa);
           ua = dr.w2;
           ub = dr.w3;
-          gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
+          if (!SPIN) {
+            gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
+          } else {
+            occ_a_bit = (uint32_t)oa ^ xorv;
+            spin_ballot(g, occ, rows + (size_t)slot * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+          }
         } else {
           const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
           int ib = (int)cemc_below(dr.w1, (uint32_t)(n_present - 1));
@@ -305,14 +454,56 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
           ua = dr.x0;
           ub = dr.x1;
           // first half: site a takes B; second half: site b takes A with a already changed
-          gather_vals<R>(g, occ, bf_s, sa, A, B, -1, 0, va, nbra, lane);
-          gather_vals<R>(g, occ, bf_s, sb, B, A, sa, B, vb, nbrb, lane);
+          if (!SPIN) {
+            gather_vals<R>(g, occ, bf_s, sa, A, B, -1, 0, va, nbra, lane);
+            gather_vals<R>(g, occ, bf_s, sb, B, A, sa, B, vb, nbrb, lane);
+          } else {
+            occ_a_bit = (uint32_t)A ^ xorv;
+            spin_ballot(g, occ, g.table + (size_t)sa * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+            spin_ballot(g, occ, g.table + (size_t)sb * cpad, xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
+          }
         }
-        __syncwarp();
-        lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
-        __syncwarp();
-        const R de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb,
-                                          tD + (size_t)warp * n_eci, lane);
+        R de;
+        if (!SPIN) {
+          __syncwarp();
+          lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
+          __syncwarp();
+          de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb,
+                                    tD + (size_t)warp * n_eci, lane);
+        } else {
+          // P_k = sum over the terms of cluster ECI k of the product of the other
+          // members' spins; D_k = delta * P_k with delta = -2 s_a the spin change.
+          R *Dw = tD + (size_t)warp * n_eci;
+          const int delta = ((occ_a_bit) ? 2 : -2);
+          const int t_lo = sp_lane_term[lane], t_hi = sp_lane_term[lane + 1], first = sp_lane_first[lane];
+          const uint32_t pa = spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wa_lo, wa_hi);
+          const uint32_t pb = SWAP ? spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wb_lo, wb_hi) : 0u;
+          R sum = (R)0;
+#pragma unroll 4
+          for (int k = 0; k < sd.n_cl; ++k) {
+            const SpinEci e = sp_eci[k];
+            int P;
+            if (!SWAP) {
+              const int odd = spin_odd(pa, k, first);
+              P = e.n_pairs - 2 * (__popc(wa_lo & e.pair_lo) + __popc(wa_hi & e.pair_hi)) + e.n_multi - 2 * odd;
+            } else {
+              // P(a) - P(b after a): the term counts cancel
+              const int sl = k - first;
+              const int va_ = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
+              const int vb_ = (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
+              const int dodd = __reduce_add_sync(kFull, va_ - vb_);
+              P = -2 * (__popc(wa_lo & e.pair_lo) + __popc(wa_hi & e.pair_hi) - __popc(wb_lo & e.pair_lo) -
+                        __popc(wb_hi & e.pair_hi)) - 2 * dodd;
+            }
+            if (lane == (k & 31)) Dw[e.eci] = (R)(delta * P);
+            sum += coef_s[e.eci] * (R)P;
+          }
+          if (sd.singlet_eci >= 0) {
+            if (lane == 0) Dw[sd.singlet_eci] = (R)(SWAP ? 0 : delta);
+            if (!SWAP) sum += coef_s[sd.singlet_eci];
+          }
+          de = (R)delta * sum;
+        }
         int acc = 0;
         if (lane == 0) {
           acc = metropolis<R>(de, ua, ub, kT, inv_kT);
@@ -343,8 +534,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     }
     __syncthreads();
 
-    if (warp == 0) {
-      // ---- phase B: first trial invalidated by an earlier accept; commit the prefix --
+    if (!helper) {
+      // ---- phase B: every warp finds the first trial invalidated by an earlier
+      // accept (the committed prefix) and commits its own trial if inside it.
       const int nv = (t_end - t0) < (uint64_t)W ? (int)(t_end - t0) : W;
       bool conflict = false;
       if (lane < nv) {
@@ -357,30 +549,32 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
       }
       const unsigned cm = __ballot_sync(kFull, conflict);
       const int ks = cm ? (__ffs(cm) - 1) : nv;
-      if (lane < ks && tacc[lane]) {
-        const int sa = tsa[lane];
-        if (!SWAP) {
-          occ[sa] = (int8_t)tsb[lane];
-        } else {
-          const int sb = tsb[lane];
-          const int A = occ[sa], B = occ[sb];
-          const int la = loc[sa], lb = loc[sb];
-          occ[sa] = (int8_t)B;
-          occ[sb] = (int8_t)A;
-          trk[misc[12 + A] + la] = sb;
-          loc[sb] = la;
-          trk[misc[12 + B] + lb] = sa;
-          loc[sa] = lb;
+      if (lane == 0 && warp < ks) {
+        const int sa = tsa[warp];
+        if (tacc[warp]) {
+          if (!SWAP) {
+            occ[sa] = (int8_t)tsb[warp];
+          } else {
+            const int sb = tsb[warp];
+            const int A = occ[sa], B = occ[sb];
+            const int la = loc[sa], lb = loc[sb];
+            occ[sa] = (int8_t)B;
+            occ[sb] = (int8_t)A;
+            trk[misc[12 + A] + la] = sb;
+            loc[sb] = la;
+            trk[misc[12 + B] + lb] = sa;
+            loc[sa] = lb;
+          }
+        }
+        if (a.trace_acc) {
+          const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + warp - t_first);
+          a.trace_site[2 * idx] = sa;
+          a.trace_site[2 * idx + 1] = tsb[warp];
+          a.trace_acc[idx] = tacc[warp];
+          a.trace_de[idx] = (double)tder[warp];
         }
       }
-      if (a.trace_acc && lane < ks) {
-        const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + lane - t_first);
-        a.trace_site[2 * idx] = tsa[lane];
-        a.trace_site[2 * idx + 1] = tsb[lane];
-        a.trace_acc[idx] = tacc[lane];
-        a.trace_de[idx] = (double)tder[lane];
-      }
-      if (lane == 0) misc[0] = ks;
+      if (warp == 0 && lane == 0) misc[0] = ks;
     }
     __syncthreads();
     const int ks = misc[0];
@@ -407,6 +601,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
       sl[i] = loc[i];
     }
   }
+  if (DF) {
+    // apply the launch's correlation-function deltas (exact sums for integer-valued changes)
+    for (int k = tid; k < n_eci; k += blockDim.x) {
+      const int kind = kind_s[k];
+      const double d = df_to(dcf[k]);
+      if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
+      else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
+    }
+    __syncthreads();
+  }
   for (int k = tid; k < n_eci; k += blockDim.x) a.cf[(size_t)chain * n_eci + k] = cf_s[k];
   if (helper && lane == 0) {
     // energy = N * eci . cf in sorted-name order (ce_updater.cpp:236-242)
@@ -416,12 +620,14 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
     a.trial[chain] = t_end;
     if (a.accum) {
       cemc_accum *ac = a.accum + acc_row;
-      ac->sum_e += acc_s[0];
-      ac->sum_e2 += acc_s[1];
+      double v[NACC];
+      for (int i = 0; i < NACC; ++i) v[i] = DF ? df_to(accd[i]) : acc_s[i];
+      ac->sum_e += v[0];
+      ac->sum_e2 += v[1];
       for (int b = 0; b < g.n_bf; ++b) {
-        ac->sum_s[b] += acc_s[2 + b];
-        ac->sum_s2[b] += acc_s[2 + CEMC_MAX_BF + b];
-        ac->sum_se[b] += acc_s[2 + 2 * CEMC_MAX_BF + b];
+        ac->sum_s[b] += v[2 + b];
+        ac->sum_s2[b] += v[2 + CEMC_MAX_BF + b];
+        ac->sum_se[b] += v[2 + 2 * CEMC_MAX_BF + b];
       }
       ac->n_samples += my_trials;
       ac->n_accept += n_acc_launch;
@@ -430,21 +636,29 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a) {
   }
 }
 
-template <typename R, int MOVE>
-static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st) {
-  auto k = mc_kernel<R, MOVE>;
+template <typename R, int MOVE, bool SPIN>
+static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
+  auto k = mc_kernel<R, MOVE, SPIN>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<a.n_chains, (a.warps + 1) * 32, smem, st>>>(g, a);
+  k<<<a.n_chains, (a.warps + 1) * 32, smem, st>>>(g, a, sd);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st) {
+template <bool SPIN>
+static cudaError_t launch_p(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
+                            const SpinDev &sd) {
   if (precision == CEMC_PREC_F32)
-    return move == CEMC_MOVE_SWAP ? launch_t<float, CEMC_MOVE_SWAP>(g, a, smem, st)
-                                  : launch_t<float, CEMC_MOVE_FLIP>(g, a, smem, st);
-  return move == CEMC_MOVE_SWAP ? launch_t<double, CEMC_MOVE_SWAP>(g, a, smem, st)
-                                : launch_t<double, CEMC_MOVE_FLIP>(g, a, smem, st);
+    return move == CEMC_MOVE_SWAP ? launch_t<float, CEMC_MOVE_SWAP, SPIN>(g, a, smem, st, sd)
+                                  : launch_t<float, CEMC_MOVE_FLIP, SPIN>(g, a, smem, st, sd);
+  return move == CEMC_MOVE_SWAP ? launch_t<double, CEMC_MOVE_SWAP, SPIN>(g, a, smem, st, sd)
+                                : launch_t<double, CEMC_MOVE_FLIP, SPIN>(g, a, smem, st, sd);
+}
+
+cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
+                      const SpinDev *spin) {
+  if (spin) return launch_p<true>(g, a, move, precision, smem, st, *spin);
+  return launch_p<false>(g, a, move, precision, smem, st, SpinDev{});
 }
 
 }  // namespace cemc

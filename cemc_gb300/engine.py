@@ -22,6 +22,9 @@ MOVE_FLIP = _lib.MOVE_FLIP
 MOVE_SWAP = _lib.MOVE_SWAP
 PREC_F64 = _lib.PREC_F64
 PREC_F32 = _lib.PREC_F32
+KERNEL_AUTO = _lib.KERNEL_AUTO
+KERNEL_GENERIC = _lib.KERNEL_GENERIC
+KERNEL_SPIN = _lib.KERNEL_SPIN
 ACCUM_DOUBLES = _lib.ACCUM_DOUBLES
 # Field offsets (in doubles) of cemc_accum.
 A_EREF, A_SUM_E, A_SUM_E2, A_SUM_S, A_SUM_S2, A_SUM_SE, A_NSAMP, A_NACC = 0, 1, 2, 3, 7, 11, 15, 16
@@ -222,7 +225,7 @@ class ChainBatch:
 
     # -- library calls -----------------------------------------------------
     def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
-            chain_trials: Optional[torch.Tensor] = None):
+            chain_trials: Optional[torch.Tensor] = None, kernel: int = 0):
         """Run ``n_trials`` trials on every chain in one launch (``cemc_run``).
 
         ``chain_trials`` (device int64, one per chain, each <= n_trials) gives chains their own counts.
@@ -238,7 +241,7 @@ class ChainBatch:
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
-                         _ptr(chain_trials))
+                         _ptr(chain_trials), int(kernel))
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         if trace:

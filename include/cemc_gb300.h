@@ -132,7 +132,17 @@ typedef struct {
                                 lets a temperature ladder keep its sums per temperature */
   const uint64_t *chain_trials; /* [n_chains] trials of each chain in this launch (device, each <= n_trials),
                                    NULL = n_trials for every chain; lets a batch mix jobs with different budgets */
+  int32_t kernel;      /* CEMC_KERNEL_*: which implementation runs the trials */
 } cemc_run_desc;
+
+/* Kernel selection of cemc_run.  AUTO takes the binary spin-basis kernel when
+ * the geometry allows it (two species with basis values +1 and -1, at most 64
+ * neighbour columns, at most 32 cluster ECIs), else the generic one.  Both give
+ * the same decisions for the same stream; the spin kernel evaluates one trial
+ * per lane with bit-packed neighbourhoods. */
+#define CEMC_KERNEL_AUTO 0
+#define CEMC_KERNEL_GENERIC 1
+#define CEMC_KERNEL_SPIN 2
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
  * energy change, accept test and in-place commit of occupation, correlation

@@ -41,17 +41,28 @@ def _cf_close(a, b, rtol=FP64_RTOL, atol=1e-14):
     return np.allclose(a, b, rtol=rtol, atol=atol)
 
 
-@pytest.mark.parametrize("warps", [1, 16, 32])
+def _kernel_ok(m, kernel, E):
+    """The spin-basis kernel only takes binary +1/-1 geometries."""
+    if kernel == E.KERNEL_SPIN and not (m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0]):
+        pytest.skip("spin-basis kernel needs a binary +1/-1 basis")
+
+
+KERNELS = [1, 2]  # generic, spin
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("warps", [1, 16, 31])
 @pytest.mark.parametrize("case", golden_cases())
-def test_gpu_replays_reference_fixture_fp64(case, warps, E):
+def test_gpu_replays_reference_fixture_fp64(case, warps, kernel, E):
     g = load_golden(case)
     s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E)
     geo = E.Geometry(m)
     move = int(g["move"])
     cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=int(g["seed"]))
     assert _cf_close(cb.cf.cpu().numpy()[0], g["cf0"], atol=1e-15)
     n = int(g["n_trials"])
-    sites, acc, de = cb.run(n, precision=E.PREC_F64, warps=warps, trace=True)
+    sites, acc, de = cb.run(n, precision=E.PREC_F64, warps=warps, trace=True, kernel=kernel)
     _sync()
     cb.check_status()
     assert np.array_equal(sites.cpu().numpy()[0], g["sites"])
@@ -62,14 +73,16 @@ def test_gpu_replays_reference_fixture_fp64(case, warps, E):
     assert np.max(np.abs(de.cpu().numpy()[0] - g["ref_de"])) < 1e-9
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("case", golden_cases())
-def test_gpu_fp32_energy_change_against_reference_fixture(case, E):
+def test_gpu_fp32_energy_change_against_reference_fixture(case, kernel, E):
     g = load_golden(case)
     s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E)
     geo = E.Geometry(m)
     cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), int(g["move"]), seed=int(g["seed"]))
     n = int(g["n_trials"])
-    sites, acc, de = cb.run(n, precision=E.PREC_F32, warps=16, trace=True)
+    sites, acc, de = cb.run(n, precision=E.PREC_F32, warps=16, trace=True, kernel=kernel)
     _sync()
     acc = acc.cpu().numpy()[0]
     de = de.cpu().numpy()[0]
@@ -143,9 +156,10 @@ def test_gpu_full_recompute_matches_oracle(recipe, E, oracle_mod):
         assert _rel(cb.energy.cpu().numpy()[c], orc.energy(m.eci_vector(eci), full)) < 1e-12
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("move", [0, 1])
 @pytest.mark.parametrize("prec", [0, 1])
-def test_gpu_batch_equals_oracle_per_chain(move, prec, E, oracle_mod):
+def test_gpu_batch_equals_oracle_per_chain(move, prec, kernel, E, oracle_mod):
     """Many chains in one launch, each equal to the oracle run of that chain (keys, temperatures, mu differ)."""
     g = load_golden("binary_flip")
     s, m, eci = golden_model(g)
@@ -160,7 +174,7 @@ def test_gpu_batch_equals_oracle_per_chain(move, prec, E, oracle_mod):
     keys = [11, 5, 7, 3, 13, 2]
     cb = E.ChainBatch(geo, occ, ev, KB * Ts, move, seed=99, chain_keys=keys)
     n = 2500
-    _, acc, de = cb.run(n, precision=prec, warps=8, trace=True)
+    _, acc, de = cb.run(n, precision=prec, warps=8, trace=True, kernel=kernel)
     _sync()
     acc = acc.cpu().numpy()
     de = de.cpu().numpy()
@@ -180,16 +194,17 @@ def test_gpu_batch_equals_oracle_per_chain(move, prec, E, oracle_mod):
                 assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
 
 
-def test_gpu_launch_splitting_is_invisible(E):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_gpu_launch_splitting_is_invisible(kernel, E):
     """k launches of n/k trials equal one launch of n (counter-based proposals, resident state)."""
     g = load_golden("binary_swap")
     s, m, eci = golden_model(g)
     geo = E.Geometry(m)
     a = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
     b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
-    a.run(3000, precision=0, warps=16)
+    a.run(3000, precision=0, warps=16, kernel=kernel)
     for _ in range(3):
-        b.run(1000, precision=0, warps=7)
+        b.run(1000, precision=0, warps=7, kernel=kernel)
     _sync()
     assert np.array_equal(a.occ.cpu().numpy(), b.occ.cpu().numpy())
     assert np.allclose(a.cf.cpu().numpy(), b.cf.cpu().numpy(), rtol=1e-12, atol=1e-15)
@@ -198,14 +213,15 @@ def test_gpu_launch_splitting_is_invisible(E):
     assert ha[0, E.A_NACC] == hb[0, E.A_NACC]
 
 
-def test_gpu_accumulators_match_oracle(E, oracle_mod):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_gpu_accumulators_match_oracle(kernel, E, oracle_mod):
     g = load_golden("binary_flip")
     s, m, eci = golden_model(g)
     geo = E.Geometry(m)
     orc = oracle_mod.Oracle(m)
     for prec in (0, 1):
         cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 0, seed=int(g["seed"]))
-        cb.run(3000, precision=prec, warps=16)
+        cb.run(3000, precision=prec, warps=16, kernel=kernel)
         _sync()
         st = orc.new_chain_state(g["occ0"], g["eci"], float(g["kT"]), 0)
         orc.run(st, seed=int(g["seed"]), chain_id=0, t_begin=0, n_trials=3000)
@@ -254,3 +270,13 @@ def test_gpu_replica_exchange_matches_restatement(E):
             assert np.array_equal(rep_d.cpu().numpy(), rep)
             assert np.array_equal(kT_d.cpu().numpy(), kT)
             assert int(nacc.item()) == acc
+
+
+def test_gpu_spin_kernel_rejects_ternary(E):
+    g = load_golden("ternary_flip")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 0, seed=1)
+    from cemc_gb300._lib import CemcError
+    with pytest.raises(CemcError):
+        cb.run(10, kernel=E.KERNEL_SPIN)
