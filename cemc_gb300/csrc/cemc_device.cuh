@@ -108,6 +108,23 @@ __device__ __forceinline__ df64 df_mul(df64 a, df64 b) {
   return df_norm(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
 }
 
+// Running-sum arithmetic shared by both precisions: A = double in FP64 mode,
+// df64 in FP32 mode; x is a per-trial value of the mode's type.
+__device__ __forceinline__ double acc_add(double a, double b) { return a + b; }
+__device__ __forceinline__ df64 acc_add(df64 a, df64 b) { return df_add(a, b); }
+__device__ __forceinline__ double acc_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ df64 acc_mul(df64 a, df64 b) { return df_mul(a, b); }
+__device__ __forceinline__ double acc_add_x(double a, double x) { return a + x; }
+__device__ __forceinline__ df64 acc_add_x(df64 a, float x) { return df_add(a, x); }
+__device__ __forceinline__ double acc_to(double a) { return a; }
+__device__ __forceinline__ double acc_to(df64 a) { return df_to(a); }
+template <typename A>
+__device__ __forceinline__ A acc_from(double d);
+template <>
+__device__ __forceinline__ double acc_from<double>(double d) { return d; }
+template <>
+__device__ __forceinline__ df64 acc_from<df64>(double d) { return df_from(d); }
+
 // Metropolis test of the reference, accept = (dE < 0) or (u <= exp(-dE / kT))
 // (cemc/mcmc/montecarlo.py:950-956), with u the 53-bit uniform of words (a, b).
 // The test is first made in single precision as ln(u) + dE/kT against a

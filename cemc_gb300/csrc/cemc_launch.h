@@ -41,7 +41,7 @@ struct Draw {
 };
 
 struct McLayout {
-  size_t cf, eci, w, acc, coef, bf, terms, lane_term, kind, misc;
+  size_t cf, eci, w, acc, cfw, coef, bf, terms, lane_term, kind, misc;
   size_t sp_eci, sp_masks, sp_shift, sp_lane;  // spin-basis tables (empty unless n_cl > 0)
   size_t rec, rec_stride, rec_tsa, rec_tsb, rec_acc, rec_der, rec_de, rec_d;
   size_t draws, rows;
@@ -65,8 +65,10 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 8 * K);
   L.w = o;
   o = align16(o + 8 * K);
-  L.acc = o;  // running sums (14), singlets at launch start (4), 1/N, then per-ECI launch deltas (n_eci)
-  o = align16(o + 8 * (size_t)(2 + 3 * CEMC_MAX_BF + CEMC_MAX_BF + 1 + K));
+  L.acc = o;  // per-lane running sums [14][32], then singlets at launch start (4) and 1/N
+  o = align16(o + 8 * (size_t)((2 + 3 * CEMC_MAX_BF) * 32 + CEMC_MAX_BF + 1));
+  L.cfw = o;  // per-warp sums of committed correlation-function changes [warps][n_eci]
+  o = align16(o + 8 * (size_t)warps * K);
   L.coef = o;
   o = align16(o + (size_t)rsize * K);
   L.bf = o;

@@ -28,9 +28,14 @@
 // counter-based draws (philox.h) of upcoming trials, prefetches their
 // neighbour-table rows from L2/HBM into a shared-memory ring with cp.async two
 // rounds ahead (single-site flips, whose site does not depend on the state),
-// and folds the previous round's accepted changes into the FP64 correlation
-// functions, energy and running sums (double-buffered trial records).
+// and folds the previous round's records (double-buffered) into per-lane
+// running sums of energy and singlets.  Each evaluating warp adds the
+// correlation-function changes of its own committed accepted trials to
+// per-warp sums; the correlation functions and the energy are brought up to
+// date in FP64 once, at the end of the launch.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "cemc_device.cuh"
 #include "cemc_launch.h"
@@ -123,13 +128,18 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   double *cf_s = reinterpret_cast<double *>(smem + L.cf);
   double *eci_s = reinterpret_cast<double *>(smem + L.eci);
   double *w_s = reinterpret_cast<double *>(smem + L.w);
-  // Running sums of this launch: FP64 in FP64 mode; double-float in FP32 mode, where
-  // the correlation functions also accumulate per-launch deltas (applied in the epilogue).
+  // Running sums of this launch, FP64 in FP64 mode and double-float in FP32
+  // mode.  The thermodynamic sums are kept per lane of the helper warp (lane =
+  // position of a trial in its round) and the committed correlation-function
+  // changes per evaluating warp, so no round needs a cross-lane or cross-warp
+  // reduction of them; both are reduced once, in fixed order, in the epilogue.
   constexpr bool DF = (sizeof(R) == 4);
+  using A = typename std::conditional<DF, df64, double>::type;
   constexpr int NACC = 2 + 3 * CEMC_MAX_BF;
-  double *acc_s = reinterpret_cast<double *>(smem + L.acc);
-  df64 *accd = reinterpret_cast<df64 *>(smem + L.acc);      // [NACC] sums, [NACC..+4) singlet starts, [NACC+4] 1/N
-  df64 *dcf = accd + NACC + CEMC_MAX_BF + 1;                // [n_eci] launch deltas (FP32 mode)
+  constexpr int NBF = SPIN ? 1 : CEMC_MAX_BF;
+  A *lacc = reinterpret_cast<A *>(smem + L.acc);  // [NACC][32]
+  A *s_start = lacc + NACC * 32;                  // [CEMC_MAX_BF] singlets at launch start, then 1/N
+  A *cfw = reinterpret_cast<A *>(smem + L.cfw);   // [W][n_eci]
   R *coef_s = reinterpret_cast<R *>(smem + L.coef);
   R *bf_s = reinterpret_cast<R *>(smem + L.bf);
   uint16_t *terms_s = reinterpret_cast<uint16_t *>(smem + L.terms);
@@ -168,8 +178,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   for (int k = tid; k < n_eci; k += blockDim.x) {
     const int kind = g.eci_kind[k];
     const double e = a.eci[(size_t)chain * n_eci + k];
-    if (DF) dcf[k] = df64{0.f, 0.f};
-    cf_s[k] = a.cf[(size_t)chain * n_eci + k];
+    cf_s[k] =a.cf[(size_t)chain * n_eci + k];
     eci_s[k] = e;
     w_s[k] = (kind == 2) ? g.eci_w[k] : 0.0;
     coef_s[k] = (R)(kind == 2 ? e * (double)N * g.eci_w[k] : (kind == 1 ? e : 0.0));
@@ -187,6 +196,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
   for (uint32_t i = tid; i <= hmask; i += blockDim.x) stamp[i] = 0u;
+  for (int i = tid; i < W * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
+  for (int i = tid; i < NACC * 32; i += blockDim.x) lacc[i] = acc_from<A>(0.0);
+  {
+    // zero the change rows of both record buffers (the spin path writes only
+    // the entries of cluster and singlet ECIs)
+    for (int i = tid; i < 2 * 32 * n_eci; i += blockDim.x) {
+      const int buf = i / (32 * n_eci), j = i - buf * 32 * n_eci;
+      reinterpret_cast<R *>(rec0 + (size_t)buf * L.rec_stride + L.rec_d)[j] = (R)0;
+    }
+  }
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
     for (int t = tid; t < sd.n_masks; t += blockDim.x) {
@@ -220,14 +239,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       misc[2] = np;
       if (np < 2) misc[1] = CEMC_ERR_STATE;
     }
-    if (DF) {
-      for (int i = 0; i < NACC; ++i) accd[i] = df64{0.f, 0.f};
-      for (int b = 0; b < CEMC_MAX_BF; ++b)
-        accd[NACC + b] = b < g.n_bf ? df_from(a.cf[(size_t)chain * n_eci + g.singlet_eci[b]]) : df64{0.f, 0.f};
-      accd[NACC + CEMC_MAX_BF] = df_from(1.0 / (double)N);
-    } else {
-      for (int i = 0; i < NACC; ++i) acc_s[i] = 0.0;
-    }
+    for (int b = 0; b < CEMC_MAX_BF; ++b)
+      s_start[b] = acc_from<A>(b < g.n_bf ? a.cf[(size_t)chain * n_eci + g.singlet_eci[b]] : 0.0);
+    s_start[CEMC_MAX_BF] = acc_from<A>(1.0 / (double)N);
   }
 
   const double kT = a.kT[chain];
@@ -244,9 +258,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   const int acc_row = a.accum_slot ? a.accum_slot[chain] : chain;
   const double e_ref = a.accum ? a.accum[acc_row].e_ref : 0.0;
 
-  // Helper-warp state.
-  double energy = a.energy[chain];                               // FP64 mode: E
-  df64 eoff = DF ? df_from(a.energy[chain] - e_ref) : df64{0.f, 0.f};  // FP32 mode: E - e_ref
+  // Helper-warp state: energy relative to e_ref and, per singlet, the launch's
+  // summed singlet changes (the singlet after a trial is start + sum / N).
+  A eoff = acc_from<A>(a.energy[chain] - e_ref);
+  A dsum[NBF];
+#pragma unroll
+  for (int b = 0; b < NBF; ++b) dsum[b] = acc_from<A>(0.0);
   uint64_t n_acc_launch = 0;
   uint64_t fill_end = t_first;
 
@@ -281,121 +298,57 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     cp_async_commit();
   };
 
-  // Fold round records (buffer `rec`, `ks` committed trials) into the FP64 state.
-  // Lanes are trials; every per-round total is a warp reduction, several
-  // interleaved, and the FP64 folds are independent of each other.
+  // Fold round records (buffer `rec`, `ks` committed trials) into the running
+  // sums.  Lane j handles trial j of the round: one inclusive scan gives the
+  // energy and singlet offsets after each trial, and each lane adds its own
+  // values to its own sums; a round without accepted trials needs no scan.
   auto book = [&](const unsigned char *rec, int ks) {
     const int8_t *tacc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
     const R *tder = reinterpret_cast<const R *>(rec + L.rec_der);
     const R *tD = reinterpret_cast<const R *>(rec + L.rec_d);
     const bool mine = lane < ks;
     const bool acc = mine && tacc[lane];
-    n_acc_launch += (uint64_t)__popc(__ballot_sync(kFull, acc));
-    const R *Dl = tD + (size_t)lane * n_eci;
-    constexpr int NS = 1 + CEMC_MAX_BF;  // energy offset and singlet offsets, scanned together
-    R sc[NS];
-    sc[0] = acc ? tder[lane] : (R)0;
+    const unsigned am = __ballot_sync(kFull, acc);
+    n_acc_launch += (uint64_t)__popc(am);
+    if (!a.accum) return;
+    R x = acc ? tder[lane] : (R)0;
+    R ds[NBF];
 #pragma unroll
-    for (int b = 0; b < CEMC_MAX_BF; ++b) sc[1 + b] = (acc && b < g.n_bf) ? Dl[g.singlet_eci[b]] : (R)0;
+    for (int b = 0; b < NBF; ++b) ds[b] = (acc && b < g.n_bf) ? tD[(size_t)lane * n_eci + g.singlet_eci[b]] : (R)0;
+    if (am) {
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+      for (int o = 1; o < 32; o <<= 1) {
+        const R nx = __shfl_up_sync(kFull, x, o);
+        R nd[NBF];
 #pragma unroll
-      for (int q = 0; q < NS; ++q) {
-        const R n = __shfl_up_sync(kFull, sc[q], o);
-        if (lane >= o) sc[q] += n;
-      }
-    }
-    const R x_tot = __shfl_sync(kFull, sc[0], ks - 1);
-    if (a.accum) {
-      // sums over the round of X, X^2 and, per singlet, DS, DS^2, DS*X (X, DS: offsets after each trial)
-      constexpr int NR = 2 + 3 * CEMC_MAX_BF;
-      R r[NR];
-      const R X = sc[0];
-      r[0] = mine ? X : (R)0;
-      r[1] = mine ? X * X : (R)0;
+        for (int b = 0; b < NBF; ++b) nd[b] = __shfl_up_sync(kFull, ds[b], o);
+        if (lane >= o) {
+          x += nx;
 #pragma unroll
-      for (int b = 0; b < CEMC_MAX_BF; ++b) {
-        const R DS = sc[1 + b];
-        r[2 + 3 * b] = mine ? DS : (R)0;
-        r[3 + 3 * b] = mine ? DS * DS : (R)0;
-        r[4 + 3 * b] = mine ? DS * X : (R)0;
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int q = 0; q < NR; ++q) r[q] += __shfl_xor_sync(kFull, r[q], o);
-      }
-      if (lane == 0) {
-        if constexpr (DF) {
-          const float k = (float)ks, sX = (float)r[0], sX2 = (float)r[1];
-          const df64 ea = eoff, inv_n = accd[NACC + CEMC_MAX_BF];
-          accd[0] = df_add(df_add(accd[0], df_mul(ea, k)), sX);
-          accd[1] = df_add(df_add(df_add(accd[1], df_mul(df_mul(ea, ea), k)), df_mul(ea, 2.0f * sX)), sX2);
-#pragma unroll
-          for (int b = 0; b < CEMC_MAX_BF; ++b) {
-            if (b < g.n_bf) {
-              const df64 s0 = df_add(accd[NACC + b], df_mul(dcf[g.singlet_eci[b]], inv_n));
-              const df64 sD = df_mul(inv_n, (float)r[2 + 3 * b]);
-              const df64 sD2 = df_mul(df_mul(inv_n, inv_n), (float)r[3 + 3 * b]);
-              const df64 sDX = df_mul(inv_n, (float)r[4 + 3 * b]);
-              accd[2 + b] = df_add(df_add(accd[2 + b], df_mul(s0, k)), sD);
-              accd[2 + CEMC_MAX_BF + b] =
-                  df_add(df_add(df_add(accd[2 + CEMC_MAX_BF + b], df_mul(df_mul(s0, s0), k)), df_mul(df_mul(s0, sD), 2.0f)),
-                         sD2);
-              accd[2 + 2 * CEMC_MAX_BF + b] = df_add(
-                  df_add(df_add(df_add(accd[2 + 2 * CEMC_MAX_BF + b], df_mul(df_mul(s0, ea), k)), df_mul(s0, sX)),
-                         df_mul(ea, sD)),
-                  sDX);
-            }
-          }
-        } else {
-          const double ea = energy - e_ref, k = (double)ks, sX = (double)r[0], sX2 = (double)r[1];
-          const double inv_n = 1.0 / (double)N;
-          acc_s[0] += k * ea + sX;
-          acc_s[1] += k * ea * ea + 2.0 * ea * sX + sX2;
-#pragma unroll
-          for (int b = 0; b < CEMC_MAX_BF; ++b) {
-            if (b < g.n_bf) {
-              const double s0 = cf_s[g.singlet_eci[b]], sD = (double)r[2 + 3 * b] * inv_n;
-              const double sD2 = (double)r[3 + 3 * b] * inv_n * inv_n, sDX = (double)r[4 + 3 * b] * inv_n;
-              acc_s[2 + b] += k * s0 + sD;
-              acc_s[2 + CEMC_MAX_BF + b] += k * s0 * s0 + 2.0 * s0 * sD + sD2;
-              acc_s[2 + 2 * CEMC_MAX_BF + b] += k * s0 * ea + s0 * sX + ea * sD + sDX;
-            }
-          }
+          for (int b = 0; b < NBF; ++b) ds[b] += nd[b];
         }
       }
     }
-    __syncwarp();
-    // correlation functions: per-ECI totals of the round's committed accepted changes
-    for (int k0 = 0; k0 < n_eci; k0 += 4) {
-      R v[4];
+    if (mine) {
+      const A ve = acc_add_x(eoff, x);
+      lacc[lane] = acc_add(lacc[lane], ve);
+      lacc[32 + lane] = acc_add(lacc[32 + lane], acc_mul(ve, ve));
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = (acc && k0 + q < n_eci) ? Dl[k0 + q] : (R)0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] += __shfl_xor_sync(kFull, v[q], o);
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int k = k0 + q;
-        if (lane == q && k < n_eci) {
-          if constexpr (DF) {
-            dcf[k] = df_add(dcf[k], (float)v[q]);
-          } else {
-            const int kind = kind_s[k];
-            if (kind == 2) cf_s[k] = cf_s[k] + (double)v[q] * w_s[k];
-            else if (kind == 1) cf_s[k] = cf_s[k] + (double)v[q] / (double)N;
-          }
+      for (int b = 0; b < NBF; ++b) {
+        if (b < g.n_bf) {
+          const A vs = acc_add(s_start[b], acc_mul(acc_add_x(dsum[b], ds[b]), s_start[CEMC_MAX_BF]));
+          A *l = lacc + (2 + b) * 32 + lane;
+          l[0] = acc_add(l[0], vs);
+          l[CEMC_MAX_BF * 32] = acc_add(l[CEMC_MAX_BF * 32], acc_mul(vs, vs));
+          l[2 * CEMC_MAX_BF * 32] = acc_add(l[2 * CEMC_MAX_BF * 32], acc_mul(vs, ve));
         }
       }
     }
-    if constexpr (DF)
-      eoff = df_add(eoff, (float)x_tot);
-    else
-      energy += (double)x_tot;
-    __syncwarp();
+    if (am) {
+      eoff = acc_add_x(eoff, __shfl_sync(kFull, x, ks - 1));
+#pragma unroll
+      for (int b = 0; b < NBF; ++b) dsum[b] = acc_add_x(dsum[b], __shfl_sync(kFull, ds[b], ks - 1));
+    }
   };
 
   __syncthreads();
@@ -574,6 +527,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           a.trace_de[idx] = (double)tder[warp];
         }
       }
+      if (warp < ks && tacc[warp]) {
+        // this warp's committed accepted trial: add its change row to the warp's sums
+        const R *Dw = tD + (size_t)warp * n_eci;
+        A *cw = cfw + (size_t)warp * n_eci;
+        for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], Dw[k]);
+      }
       if (warp == 0 && lane == 0) misc[0] = ks;
     }
     __syncthreads();
@@ -601,17 +560,27 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       sl[i] = loc[i];
     }
   }
-  if (DF) {
-    // apply the launch's correlation-function deltas (exact sums for integer-valued changes)
-    for (int k = tid; k < n_eci; k += blockDim.x) {
-      const int kind = kind_s[k];
-      const double d = df_to(dcf[k]);
-      if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
-      else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
-    }
-    __syncthreads();
+  // apply the launch's correlation-function changes: the per-warp sums in warp
+  // order (exact for integer-valued changes), then one scaling per ECI
+  for (int k = tid; k < n_eci; k += blockDim.x) {
+    const int kind = kind_s[k];
+    double d = 0.0;
+    for (int w = 0; w < W; ++w) d += acc_to(cfw[(size_t)w * n_eci + k]);
+    if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
+    else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
   }
+  __syncthreads();
   for (int k = tid; k < n_eci; k += blockDim.x) a.cf[(size_t)chain * n_eci + k] = cf_s[k];
+  if (a.accum && tid < NACC) {
+    // running sum `tid` over the helper's lanes, in lane order
+    const int b = tid < 2 ? 0 : (tid - 2) % CEMC_MAX_BF;
+    if (tid < 2 || b < g.n_bf) {
+      double v = 0.0;
+      for (int l = 0; l < 32; ++l) v += acc_to(lacc[tid * 32 + l]);
+      double *sums = &a.accum[acc_row].sum_e;  // sum_e, sum_e2, sum_s[], sum_s2[], sum_se[] in NACC order
+      sums[tid] += v;
+    }
+  }
   if (helper && lane == 0) {
     // energy = N * eci . cf in sorted-name order (ce_updater.cpp:236-242)
     double e = 0.0;
@@ -620,15 +589,6 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     a.trial[chain] = t_end;
     if (a.accum) {
       cemc_accum *ac = a.accum + acc_row;
-      double v[NACC];
-      for (int i = 0; i < NACC; ++i) v[i] = DF ? df_to(accd[i]) : acc_s[i];
-      ac->sum_e += v[0];
-      ac->sum_e2 += v[1];
-      for (int b = 0; b < g.n_bf; ++b) {
-        ac->sum_s[b] += v[2 + b];
-        ac->sum_s2[b] += v[2 + CEMC_MAX_BF + b];
-        ac->sum_se[b] += v[2 + 2 * CEMC_MAX_BF + b];
-      }
       ac->n_samples += my_trials;
       ac->n_accept += n_acc_launch;
     }
