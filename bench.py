@@ -259,6 +259,66 @@ def run_served(args):
     return 0
 
 
+def run_recompute(args):
+    """Full correlation-function recompute (cemc_recompute) alone, on the ladder geometry.
+
+    Binary FCC 32x32x32 conventional (131072 sites), pairs to the 6th shell,
+    triplets to the 2nd, the nearest-neighbour tetrahedron; 48 chains with
+    random 50/50 occupations.  Algorithmic bytes per chain: N * (1 + 4 * n_cols)
+    (each site's occupation and its neighbour-table row), plus 8 * n_eci written.
+    """
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cemc_gb300 import engine as E
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    n_chains = args.recompute_chains
+    s = fcc_settings(args.recompute_cell, 6, 2, 1, SPECIES)
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m, dev)
+    rng = np.random.default_rng(rank)
+    occ = rng.integers(0, 2, (n_chains, m.n_sites)).astype(np.int8)
+    ev = np.tile(m.eci_vector(eci), (n_chains, 1))
+    cb = E.ChainBatch(geo, occ, ev, KB * 800.0, E.MOVE_FLIP, seed=1)
+    stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            cb.recompute()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                cb.recompute()
+                b.record(stream)
+            stream.synchronize()
+            times.append(a.elapsed_time(b) * 1e-3)
+    t = statistics.median(times)
+    alg_bytes = n_chains * (m.n_sites * (1 + 4 * m.n_cols) + 8 * m.n_eci)
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / t / 1e9
+    if rank == 0:
+        print(json.dumps({"metric": "full correlation-function recompute, algorithmic GB/s", "workload": "recompute",
+                          "value": achieved, "unit": "GB/s", "ms_per_call": t * 1e3,
+                          "sites_per_s": n_chains * m.n_sites / t, "steps": args.steps, "warmup": args.warmup,
+                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                       "frac": achieved / peak, "peak_kind": peak_kind,
+                                       "alg_bytes_per_call": alg_bytes},
+                          "clocks": clk.summary(),
+                          "config": {"workload": "recompute_fcc_binary_%dx%dx%d_%dchains" % ((args.recompute_cell,) * 3
+                                                                                             + (n_chains,)),
+                                     "n_sites": m.n_sites, "n_cols": m.n_cols, "n_eci": m.n_eci,
+                                     "n_chains": n_chains, "l2": "flushed before every call (256 MB write)"}}))
+    return 0
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -457,8 +517,11 @@ def main(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)
     p.add_argument("--no-correctness", action="store_true")
-    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served"],
-                   help="sgc64: the headline 64-chain batch; served: the Poisson job stream")
+    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served", "recompute"],
+                   help="sgc64: the headline 64-chain batch; served: the Poisson job stream; "
+                        "recompute: the full correlation-function recompute alone")
+    p.add_argument("--recompute-cell", type=int, default=32)
+    p.add_argument("--recompute-chains", type=int, default=48)
     p.add_argument("--served-jobs", type=int, default=300)
     p.add_argument("--served-sweep-scale", type=float, default=0.1,
                    help="scale of the served jobs' sweep budgets (1 = 10^2-10^4 sweeps)")
@@ -471,6 +534,8 @@ def main(argv=None):
         return run_reference(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "recompute":
+        return run_recompute(args)
     return run_gpu(args)
 
 

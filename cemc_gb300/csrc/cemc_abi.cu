@@ -296,6 +296,11 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.fterms = reinterpret_cast<const uint8_t *>(base + parts[11].off);
   g.fterm_off = reinterpret_cast<const int32_t *>(base + parts[12].off);
   for (int b = 0; b < CEMC_MAX_BF; ++b) g.singlet_eci[b] = singlet[b];
+  g.pm1_minus = -1;
+  if (B == 1 && S == 2) {
+    if (d->bf[0] == 1.0 && d->bf[1] == -1.0) g.pm1_minus = 1;
+    else if (d->bf[0] == -1.0 && d->bf[1] == 1.0) g.pm1_minus = 0;
+  }
   geo->spin_ok = spin_ok;
   geo->spin.n_cl = spin_ok ? (int)spin_eci.size() : 0;
   geo->spin.n_masks = spin_ok ? n_masks : 0;

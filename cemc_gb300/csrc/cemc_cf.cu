@@ -46,54 +46,91 @@ double *noalloc_scratch(cudaError_t *err) {
 // Full recompute.  Block (bx, chain) handles sites [bx*256, bx*256+256) of one
 // chain: it stages the species of every neighbour column of its sites in
 // shared memory (coalesced reads of the column-major table), then walks the
-// cluster terms ECI by ECI, one site per thread, in FP64.  Per-block sums go
-// to scratch[(chain * n_blocks + bx) * n_eci + k] and are combined in block
-// order by recompute_finish, so the result is deterministic.
+// cluster terms ECI by ECI, one site per thread.  A binary geometry whose
+// basis values are exactly +1 and -1 (g.pm1_minus >= 0) stages one "is the -1
+// species" bit per column instead and takes the sign of each product as the
+// parity of its members' bits: integer sums, exact, with no FP64 arithmetic.
+// Other bases multiply their FP64 basis values.  Each warp's sum of an ECI
+// goes to shared memory; after the last ECI thread k adds the eight warps in
+// order into scratch[(chain * n_blocks + bx) * n_eci + k], and recompute_finish
+// adds the blocks in order, so the result is deterministic.
 constexpr int kCfThreads = 256;
 
+template <bool PM1>
 __global__ void __launch_bounds__(kCfThreads) recompute_partial(DevGeo g, const int8_t *occ_all, double *scratch,
                                                                 int n_blocks) {
   extern __shared__ __align__(16) unsigned char smem[];
-  int8_t *nb = reinterpret_cast<int8_t *>(smem);                              // [n_cols][256]
-  double *red = reinterpret_cast<double *>(smem + align16((size_t)g.n_cols * kCfThreads));  // [8]
-  double *bf_s = red + 8;                                                     // [n_bf * n_sym]
+  int8_t *nb = reinterpret_cast<int8_t *>(smem);  // [n_cols][256] species, or -1-species bits
+  double *red = reinterpret_cast<double *>(smem + align16((size_t)g.n_cols * kCfThreads));  // [8][n_eci]
+  double *bf_s = red + (kCfThreads / 32) * g.n_eci;                                        // [n_bf * n_sym]
   const int chain = blockIdx.y, bx = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int N = g.n_sites;
   const int i = bx * kCfThreads + tid;
   const bool valid = i < N;
   const int8_t *occ = occ_all + (size_t)chain * N;
-  for (int q = tid; q < g.n_bf * g.n_sym; q += kCfThreads) bf_s[q] = g.bf[q];
-  for (int c = 0; c < g.n_cols; ++c) nb[c * kCfThreads + tid] = valid ? occ[g.table_cm[(size_t)c * N + i]] : 0;
+  const int minus = g.pm1_minus;
+  if (!PM1)
+    for (int q = tid; q < g.n_bf * g.n_sym; q += kCfThreads) bf_s[q] = g.bf[q];
+  for (int c = 0; c < g.n_cols; ++c) {
+    int8_t v = 0;
+    if (valid) {
+      const int o = occ[g.table_cm[(size_t)c * N + i]];
+      v = PM1 ? (int8_t)(o == minus) : (int8_t)o;
+    }
+    nb[c * kCfThreads + tid] = v;
+  }
   const int me = valid ? occ[i] : 0;
+  const int me_bit = (me == minus) ? 1 : 0;
   __syncthreads();
   for (int k = 0; k < g.n_eci; ++k) {
     const int kind = g.eci_kind[k];
-    double s = 0.0;
-    if (valid && kind == 1) {
-      s = bf_s[g.eci_dec[k] * g.n_sym + me];
-    } else if (valid && kind == 2) {
-      const int f0 = g.fterm_off[k], f1 = g.fterm_off[k + 1];
-      for (int f = f0; f < f1; ++f) {
-        const uint2 t = __ldg(reinterpret_cast<const uint2 *>(g.fterms) + f);
-        const int c0 = t.x & 0xff, c1 = (t.x >> 8) & 0xff, c2 = (t.x >> 16) & 0xff;
-        const int d0 = (t.x >> 24) & 0xff, d1 = t.y & 0xff, d2 = (t.y >> 8) & 0xff, dr = (t.y >> 16) & 0xff;
-        const int size = (t.y >> 24) & 0xff;
-        double p = bf_s[dr * g.n_sym + me] * bf_s[d0 * g.n_sym + nb[c0 * kCfThreads + tid]];
-        if (size >= 3) p *= bf_s[d1 * g.n_sym + nb[c1 * kCfThreads + tid]];
-        if (size >= 4) p *= bf_s[d2 * g.n_sym + nb[c2 * kCfThreads + tid]];
-        s += p;
-      }
-    }
     if (kind == 0) continue;
-    s = warp_sum(s);
-    if (lane == 0) red[warp] = s;
-    __syncthreads();
-    if (tid == 0) {
-      double b = 0.0;
-      for (int w = 0; w < kCfThreads / 32; ++w) b += red[w];
-      scratch[((size_t)chain * n_blocks + bx) * g.n_eci + k] = b;
+    const int f0 = g.fterm_off[k], f1 = g.fterm_off[k + 1];
+    double s;
+    if (PM1) {
+      int cnt = 0;
+      if (valid) {
+        if (kind == 1) {
+          cnt = 1 - 2 * me_bit;
+        } else {
+          for (int f = f0; f < f1; ++f) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(g.fterms) + f);
+            const int c0 = t.x & 0xff, c1 = (t.x >> 8) & 0xff, c2 = (t.x >> 16) & 0xff;
+            const int size = (t.y >> 24) & 0xff;
+            int bit = me_bit ^ nb[c0 * kCfThreads + tid];
+            if (size >= 3) bit ^= nb[c1 * kCfThreads + tid];
+            if (size >= 4) bit ^= nb[c2 * kCfThreads + tid];
+            cnt += 1 - 2 * bit;
+          }
+        }
+      }
+      s = (double)__reduce_add_sync(kFull, cnt);
+    } else {
+      s = 0.0;
+      if (valid && kind == 1) {
+        s = bf_s[g.eci_dec[k] * g.n_sym + me];
+      } else if (valid && kind == 2) {
+        for (int f = f0; f < f1; ++f) {
+          const uint2 t = __ldg(reinterpret_cast<const uint2 *>(g.fterms) + f);
+          const int c0 = t.x & 0xff, c1 = (t.x >> 8) & 0xff, c2 = (t.x >> 16) & 0xff;
+          const int d0 = (t.x >> 24) & 0xff, d1 = t.y & 0xff, d2 = (t.y >> 8) & 0xff, dr = (t.y >> 16) & 0xff;
+          const int size = (t.y >> 24) & 0xff;
+          double p = bf_s[dr * g.n_sym + me] * bf_s[d0 * g.n_sym + nb[c0 * kCfThreads + tid]];
+          if (size >= 3) p *= bf_s[d1 * g.n_sym + nb[c1 * kCfThreads + tid]];
+          if (size >= 4) p *= bf_s[d2 * g.n_sym + nb[c2 * kCfThreads + tid]];
+          s += p;
+        }
+      }
+      s = warp_sum(s);
     }
-    __syncthreads();
+    if (lane == 0) red[warp * g.n_eci + k] = s;
+  }
+  __syncthreads();
+  for (int k = tid; k < g.n_eci; k += kCfThreads) {
+    if (g.eci_kind[k] == 0) continue;
+    double b = 0.0;
+    for (int w = 0; w < kCfThreads / 32; ++w) b += red[w * g.n_eci + k];
+    scratch[((size_t)chain * n_blocks + bx) * g.n_eci + k] = b;
   }
 }
 
@@ -335,10 +372,12 @@ size_t recompute_blocks(const DevGeo &g) { return (size_t)((g.n_sites + kCfThrea
 cudaError_t launch_recompute(const DevGeo &g, int n_chains, const int8_t *occ, const double *eci, double *cf,
                              double *energy, double *scratch, cudaStream_t st) {
   const int nb = (int)recompute_blocks(g);
-  const size_t smem1 = align16((size_t)g.n_cols * kCfThreads) + 8 * (8 + (size_t)g.n_bf * g.n_sym);
-  cudaError_t e = cudaFuncSetAttribute(recompute_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+  const size_t smem1 =
+      align16((size_t)g.n_cols * kCfThreads) + 8 * ((kCfThreads / 32) * (size_t)g.n_eci + (size_t)g.n_bf * g.n_sym);
+  auto kern = g.pm1_minus >= 0 ? recompute_partial<true> : recompute_partial<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
   if (e != cudaSuccess) return e;
-  recompute_partial<<<dim3(nb, n_chains), kCfThreads, smem1, st>>>(g, occ, scratch, nb);
+  kern<<<dim3(nb, n_chains), kCfThreads, smem1, st>>>(g, occ, scratch, nb);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   recompute_finish<<<n_chains, 128, 8 * (size_t)g.n_eci, st>>>(g, nb, scratch, eci, cf, energy);

@@ -45,6 +45,7 @@ struct DevGeo {
   const uint8_t *fterms;    // [n_terms * 8] {col0, col1, col2, d0, d1, d2, d_ref, size}
   const int32_t *fterm_off; // [n_eci + 1] ranges of fterms per ECI
   int singlet_eci[CEMC_MAX_BF];
+  int pm1_minus;  // binary basis with values exactly +1 / -1: species id of -1; otherwise -1
 };
 
 __device__ __forceinline__ double warp_sum(double v) {

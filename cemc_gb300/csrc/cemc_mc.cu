@@ -363,6 +363,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   __syncthreads();
 
   const int n_present = SWAP ? misc[2] : 0;
+  // spin path: lane k of every evaluating warp holds cluster ECI k and its coefficient
+  SpinEci sp_e{};
+  R sp_coef = (R)0;
+  unsigned sp_multi = 0;  // cluster ECIs with multi-site terms
+  if (SPIN) {
+    if (lane < sd.n_cl) {
+      sp_e = sp_eci[lane];
+      sp_coef = coef_s[sp_e.eci];
+    }
+    sp_multi = __ballot_sync(kFull, lane < sd.n_cl && sp_e.n_multi > 0);
+  }
   uint64_t t0 = t_first;
   uint32_t round = 1;
   int ks_prev = 0;
@@ -426,31 +437,35 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         } else {
           // P_k = sum over the terms of cluster ECI k of the product of the other
           // members' spins; D_k = delta * P_k with delta = -2 s_a the spin change.
+          // Lane k evaluates cluster ECI k: its pair terms by popcounts of its shell
+          // masks, its multi-site terms from one warp reduction per ECI that has any.
           R *Dw = tD + (size_t)warp * n_eci;
           const int delta = ((occ_a_bit) ? 2 : -2);
           const int t_lo = sp_lane_term[lane], t_hi = sp_lane_term[lane + 1], first = sp_lane_first[lane];
           const uint32_t pa = spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wa_lo, wa_hi);
           const uint32_t pb = SWAP ? spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wb_lo, wb_hi) : 0u;
-          R sum = (R)0;
-#pragma unroll 4
-          for (int k = 0; k < sd.n_cl; ++k) {
-            const SpinEci e = sp_eci[k];
-            int P;
+          int my_odd = 0;
+          for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+            const int k = __ffs(mm) - 1;
+            const int sl = k - first;
+            int v = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
+            if (SWAP) v -= (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
+            const int odd = __reduce_add_sync(kFull, v);
+            if (lane == k) my_odd = odd;
+          }
+          int P = 0;
+          if (lane < sd.n_cl) {
             if (!SWAP) {
-              const int odd = spin_odd(pa, k, first);
-              P = e.n_pairs - 2 * (__popc(wa_lo & e.pair_lo) + __popc(wa_hi & e.pair_hi)) + e.n_multi - 2 * odd;
+              P = sp_e.n_pairs - 2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi)) + sp_e.n_multi -
+                  2 * my_odd;
             } else {
               // P(a) - P(b after a): the term counts cancel
-              const int sl = k - first;
-              const int va_ = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
-              const int vb_ = (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
-              const int dodd = __reduce_add_sync(kFull, va_ - vb_);
-              P = -2 * (__popc(wa_lo & e.pair_lo) + __popc(wa_hi & e.pair_hi) - __popc(wb_lo & e.pair_lo) -
-                        __popc(wb_hi & e.pair_hi)) - 2 * dodd;
+              P = -2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi) - __popc(wb_lo & sp_e.pair_lo) -
+                        __popc(wb_hi & sp_e.pair_hi)) - 2 * my_odd;
             }
-            if (lane == (k & 31)) Dw[e.eci] = (R)(delta * P);
-            sum += coef_s[e.eci] * (R)P;
+            Dw[sp_e.eci] = (R)(delta * P);
           }
+          R sum = warp_sum(sp_coef * (R)P);
           if (sd.singlet_eci >= 0) {
             if (lane == 0) Dw[sd.singlet_eci] = (R)(SWAP ? 0 : delta);
             if (!SWAP) sum += coef_s[sd.singlet_eci];
