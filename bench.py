@@ -365,6 +365,7 @@ def run_gpu(args):
     bytes_per_flip = 5 * m.n_cols + 1
     keys = np.arange(N_CHAINS) + rank * N_CHAINS
     runner = BatchRunner(geo, occ, ev, Ts, E.MOVE_FLIP, seed=2026, precision=E.PREC_F32, warps=args.warps,
+                         cluster=args.cluster,
                          sweeps_per_step=args.sweeps_per_step, recompute_every=1, graph=True, chain_keys=keys)
     stream = runner.stream
     runner.capture()
@@ -403,7 +404,8 @@ def run_gpu(args):
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile_case": True, "value": value, "unit": UNIT, "ms_per_step": t_max * 1e3 / args.steps,
-                              "warps_per_chain": runner.warps, "sweeps_per_step": args.sweeps_per_step}))
+                              "warps_per_cta": runner.warps, "ctas_per_chain": runner.cluster,
+                              "sweeps_per_step": args.sweeps_per_step}))
         if dist is not None:
             dist.barrier()
             dist.destroy_process_group()
@@ -417,7 +419,7 @@ def run_gpu(args):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             a.record(stream)
-            cb.run(runner.trials_per_step, precision=E.PREC_F32, warps=runner.warps)
+            cb.run(runner.trials_per_step, precision=E.PREC_F32, warps=runner.warps, cluster=runner.cluster)
             b.record(stream)
         stream.synchronize()
         kms.append(a.elapsed_time(b))
@@ -454,12 +456,12 @@ def run_gpu(args):
     plain = None
     if rank == 0:
         pb = E.ChainBatch(geo, occ[:1], ev[:1], KB * Ts[:1], E.MOVE_FLIP, seed=5)
-        pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps)
+        pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps, cluster=1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         n_launch = 4
         for _ in range(n_launch):
-            pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps)
+            pb.run(m.n_sites, precision=E.PREC_F64, warps=runner.warps, cluster=1)
         torch.cuda.synchronize()
         plain = n_launch * m.n_sites / (time.perf_counter() - t0)
 
@@ -484,7 +486,7 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "sgc_flip_fcc_binary_16x16x16_64chains", "n_sites": m.n_sites,
                        "n_chains": N_CHAINS, "sweeps_per_step": args.sweeps_per_step, "recompute": "fp64 every step",
-                       "warps_per_chain": runner.warps, "cuda_graph": True,
+                       "warps_per_cta": runner.warps, "ctas_per_chain": runner.cluster, "cuda_graph": True,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
             "gpu_launches": n_launches,
             "clocks": clocks,
@@ -512,7 +514,8 @@ def main(argv=None):
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--warps", type=int, default=0, help="warps per chain (0 = autotuned)")
+    p.add_argument("--warps", type=int, default=0, help="evaluating warps per CTA (0 = autotuned with --cluster)")
+    p.add_argument("--cluster", type=int, default=0, help="CTAs per chain, 1 or 2 (0 = chosen by the library)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)

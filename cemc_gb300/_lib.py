@@ -53,7 +53,7 @@ class RunDesc(C.Structure):
                 ("occ", _P), ("cf", _P), ("energy", _P), ("eci", _P), ("kT", _P), ("trial", _P), ("accum", _P),
                 ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
                 ("trace_site", _P), ("trace_acc", _P), ("trace_de", _P), ("status", _P), ("chain_key", _P),
-                ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32)]
+                ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32), ("cluster", C.c_int32)]
 
 
 class CemcError(RuntimeError):

@@ -1,24 +1,28 @@
-"""Autotuner for the speculation width (warps per chain) of the Monte Carlo kernel.
+"""Autotuner for the launch shape of the Monte Carlo kernel.
 
-The best width depends on the supercell size (conflict probability between
-trials of one round), the cluster set (work per trial), the move type and the
-number of chains sharing the GPU.  ``best_warps`` times short runs of the
-candidate widths on scratch copies of a synthetic batch and caches the winner
-in a JSON file keyed by those features and the device name.
+A launch shape is (warps, cluster): evaluating warps per CTA and CTAs per
+chain (1, or a cluster pair of 2 on two SMs).  Trials per round are their
+product.  The best shape depends on the supercell size (conflict probability
+between trials of one round), the cluster set (work per trial), the move type
+and the number of chains sharing the GPU (pairs only pay while SMs are idle).
+``best_config`` times short runs of the candidate shapes on the caller's batch
+(state restored afterwards) or on a synthetic one and caches the winner in a
+JSON file keyed by those features and the device name.
 """
 from __future__ import annotations
 
 import json
 import os
 import threading
-from typing import Dict, Optional, Sequence
+from typing import Dict, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
 
 from . import engine as E
 
-CANDIDATES = (1, 2, 4, 8, 12, 16, 24, 31)
+CANDIDATES = (4, 8, 16, 24, 30)          # warps per CTA, one CTA per chain
+PAIR_CANDIDATES = (8, 16, 24, 30)        # warps per CTA, cluster pairs
 _CACHE_PATH = os.environ.get("CEMC_AUTOTUNE_CACHE",
                              os.path.join(os.path.expanduser("~"), ".cache", "cemc_gb300", "autotune.json"))
 _lock = threading.Lock()
@@ -30,8 +34,17 @@ def _key(geo, move, precision, n_chains) -> str:
     m = geo.model
     # chains only matter up to one per SM
     sms = torch.cuda.get_device_properties(geo.device).multi_processor_count
-    return "|".join(map(str, (name, m.n_sites, m.n_cols, m.n_terms, m.n_eci, move, precision,
+    return "|".join(map(str, ("shape", name, m.n_sites, m.n_cols, m.n_terms, m.n_eci, move, precision,
                               min(int(n_chains), sms))))
+
+
+def candidates(geo, n_chains: int):
+    """(warps, cluster) shapes worth timing for ``n_chains`` chains on this device."""
+    sms = torch.cuda.get_device_properties(geo.device).multi_processor_count
+    out = [(w, 1) for w in CANDIDATES]
+    if 2 * int(n_chains) <= sms:
+        out += [(w, 2) for w in PAIR_CANDIDATES]
+    return out
 
 
 def _load():
@@ -53,9 +66,9 @@ def _save(d):
         pass
 
 
-def tune(geo, move: int, precision: int, n_chains: int, candidates: Sequence[int] = CANDIDATES,
-         sweeps: float = 0.5, seed: int = 12345) -> Dict[int, float]:
-    """Trials/s of each candidate width on a random 50/50 batch at a mid-range temperature."""
+def tune(geo, move: int, precision: int, n_chains: int, shapes=None, sweeps: float = 0.5,
+         seed: int = 12345) -> Dict[tuple, float]:
+    """Trials/s of each candidate shape on a random batch at a mid-range temperature."""
     m = geo.model
     n = min(int(n_chains), torch.cuda.get_device_properties(geo.device).multi_processor_count)
     rng = np.random.default_rng(seed)
@@ -63,57 +76,58 @@ def tune(geo, move: int, precision: int, n_chains: int, candidates: Sequence[int
     eci = np.zeros(m.n_eci)
     eci[m.eci_kind == 2] = rng.normal(0.0, 0.01, int((m.eci_kind == 2).sum()))
     cb = E.ChainBatch(geo, occ, eci, 8.6173303e-5 * 800.0, move, seed=seed)
-    trials = max(256, int(sweeps * m.n_sites))
-    out = {}
-    for w in candidates:
-        cb.run(trials // 4, precision=precision, warps=w)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        cb.run(trials, precision=precision, warps=w)
-        e1.record()
-        torch.cuda.synchronize()
-        out[int(w)] = n * trials / (e0.elapsed_time(e1) * 1e-3)
-    return out
+    return tune_on(cb, precision, shapes, sweeps)
 
 
-def tune_on(cb, precision: int, candidates: Sequence[int] = CANDIDATES, sweeps: float = 0.25) -> Dict[int, float]:
-    """Trials/s of each width on the caller's own batch; its state is restored afterwards."""
+def tune_on(cb, precision: int, shapes=None, sweeps: float = 0.25) -> Dict[tuple, float]:
+    """Trials/s of each shape on the caller's own batch; its state is restored afterwards."""
+    shapes = list(shapes) if shapes is not None else candidates(cb.geo, cb.n_chains)
     names = ["occ", "cf", "energy", "trial", "accum"] + (["trk", "loc"] if cb.trk is not None else [])
     snap = {n: getattr(cb, n).clone() for n in names}
     trials = max(256, int(sweeps * cb.geo.n_sites))
     stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
     out = {}
-    for w in candidates:
-        cb.run(trials // 4, precision=precision, warps=w)
+    from ._lib import CemcError
+    for w, cl in shapes:
+        try:
+            cb.run(trials // 4, precision=precision, warps=w, cluster=cl)
+        except CemcError as exc:
+            if exc.code == 5:  # this shape does not fit in shared memory
+                continue
+            raise
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)  # the kernel runs on the batch's stream
-        cb.run(trials, precision=precision, warps=w)
+        cb.run(trials, precision=precision, warps=w, cluster=cl)
         e1.record(stream)
         torch.cuda.synchronize()
-        out[int(w)] = cb.n_chains * trials / (e0.elapsed_time(e1) * 1e-3)
+        out[(int(w), int(cl))] = cb.n_chains * trials / (e0.elapsed_time(e1) * 1e-3)
         for n, t in snap.items():
             getattr(cb, n).copy_(t)
     torch.cuda.synchronize()
     return out
 
 
-def best_warps(geo, move: int, precision: int, n_chains: int, batch=None) -> int:
-    """Cached best width for this geometry/move/precision/chain count; tuned on ``batch`` when given."""
+def best_config(geo, move: int, precision: int, n_chains: int, batch=None) -> Tuple[int, int]:
+    """Cached best (warps, cluster) for this geometry/move/precision/chain count; tuned on ``batch`` when given."""
     key = _key(geo, move, precision, n_chains)
     with _lock:
         if key in _mem:
             return _mem[key]
         disk = _load()
         if key in disk:
-            _mem[key] = int(disk[key])
+            _mem[key] = tuple(int(x) for x in disk[key])
             return _mem[key]
     rates = tune_on(batch, precision) if batch is not None else tune(geo, move, precision, n_chains)
     best = max(rates, key=rates.get)
     with _lock:
         _mem[key] = best
         disk = _load()
-        disk[key] = best
+        disk[key] = list(best)
         _save(disk)
     return best
+
+
+def best_warps(geo, move: int, precision: int, n_chains: int, batch=None) -> int:
+    """Warps per CTA of the best shape (``best_config``)."""
+    return best_config(geo, move, precision, n_chains, batch)[0]

@@ -26,7 +26,7 @@ class BatchRunner:
     def __init__(self, geo: Geometry, occ, eci, temperatures, move: int, seed: int = 0,
                  precision: int = E.PREC_F32, warps: int = 0, sweeps_per_step: float = 1.0,
                  recompute_every: int = 1, graph: bool = True, chain_keys=None, kB: float = KB_EV,
-                 stream: Optional[torch.cuda.Stream] = None):
+                 stream: Optional[torch.cuda.Stream] = None, cluster: int = 0):
         self.geo = geo
         self.kB = kB
         self.temperatures = np.broadcast_to(np.asarray(temperatures, dtype=np.float64),
@@ -37,9 +37,10 @@ class BatchRunner:
                                  stream=self.stream)
         self.precision = int(precision)
         if warps == 0:
-            from .autotune import best_warps
-            warps = best_warps(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
+            from .autotune import best_config
+            warps, cluster = best_config(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
         self.warps = int(warps)
+        self.cluster = int(cluster)  # CTAs per chain (0: chosen by the library)
         self.trials_per_step = max(1, int(round(sweeps_per_step * geo.n_sites)))
         self.recompute_every = max(0, int(recompute_every))
         self.use_graph = bool(graph)
@@ -51,7 +52,7 @@ class BatchRunner:
         return self.cb.n_chains
 
     def _step_body(self, with_recompute: bool):
-        self.cb.run(self.trials_per_step, precision=self.precision, warps=self.warps)
+        self.cb.run(self.trials_per_step, precision=self.precision, warps=self.warps, cluster=self.cluster)
         if with_recompute:
             self.cb.recompute()
 

@@ -7,6 +7,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -44,6 +47,10 @@ struct cemc_geometry {
   bool spin_ok = false;
   void *dev = nullptr;  // one device allocation holding every table
   int max_smem = 0;     // opt-in shared memory per block of the current device
+  int n_sms = 0;        // multiprocessors of the current device
+  // resident cluster pairs per launch configuration (warps, move, precision, spin, smem)
+  mutable std::mutex mu;
+  mutable std::map<std::tuple<int, int, int, int, size_t>, int> pairs;
 };
 
 extern "C" int cemc_last_error(char *buf, size_t len) {
@@ -314,6 +321,7 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&geo->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaDeviceGetAttribute(&geo->n_sms, cudaDevAttrMultiProcessorCount, dev);
   *out = geo;
   return CEMC_OK;
 }
@@ -369,8 +377,9 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   if (r->kernel == CEMC_KERNEL_SPIN && !geo->spin_ok)
     return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
-  // Shared memory: the occupation, then (swaps) the site lists, then an exact
-  // stamp table (one entry per site) are preferred; fall back in that order.
+  if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
+  // Shared memory: the occupation, then (swaps) the site lists, then exact
+  // stamp tables (one entry per site) are preferred; fall back in that order.
   const size_t budget = (size_t)geo->max_smem;
   int exact_bits = 0;
   while ((1 << exact_bits) < g.n_sites) ++exact_bits;
@@ -380,24 +389,54 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     int occ, trk, min_bits;
   };
   const Choice choices[] = {{1, is_swap, exact_bits}, {1, 0, exact_bits}, {1, 0, 12}, {0, 0, 12}, {0, 0, 5}};
-  bool found = false;
-  cemc::McLayout L{};
-  for (const Choice &ch : choices) {
-    for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
-      L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks);
-      if (L.total <= budget) {
-        a.occ_smem = ch.occ;
-        a.trk_smem = ch.trk;
-        a.stamp_bits = bits;
-        found = true;
-        break;
+  auto fit = [&](int cl, cemc::McLayout &L, cemc::RunArgs &x) {
+    const int rb = cemc::ring_bits_for(cl);
+    for (const Choice &ch : choices) {
+      for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
+        L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, use_spin);
+        if (L.total <= budget) {
+          x.occ_smem = ch.occ;
+          x.trk_smem = ch.trk;
+          x.stamp_bits = bits;
+          x.ring_bits = rb;
+          x.cl = cl;
+          return true;
+        }
       }
     }
-    if (found) break;
+    return false;
+  };
+  // Resident cluster pairs of this configuration (cached per geometry).
+  auto resident_pairs = [&](const cemc::McLayout &L, const cemc::RunArgs &x) {
+    const auto key = std::make_tuple(warps, (int)r->move, (int)r->precision, (int)use_spin, L.total);
+    std::lock_guard<std::mutex> lock(geo->mu);
+    auto it = geo->pairs.find(key);
+    if (it != geo->pairs.end()) return it->second;
+    const int n = cemc::max_active_clusters(g, x, r->move, r->precision, L.total, use_spin);
+    geo->pairs[key] = n;
+    return n;
+  };
+  cemc::McLayout L{};
+  bool found = false;
+  if (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms)) {
+    cemc::RunArgs x = a;
+    cemc::McLayout L2{};
+    if (fit(2, L2, x)) {
+      const int n = resident_pairs(L2, x);
+      if (r->cluster == 2 && n < 1) return fail(CEMC_ERR_LIMIT, "no CTA pair of this size fits on the device");
+      if (r->cluster == 2 || n >= r->n_chains) {
+        a = x;
+        L = L2;
+        found = true;
+      }
+    } else if (r->cluster == 2) {
+      return fail(CEMC_ERR_LIMIT, "shared memory of a CTA pair exceeds %zu bytes; use fewer warps", budget);
+    }
   }
+  if (!found) found = fit(1, L, a);
   if (!found) return fail(CEMC_ERR_LIMIT, "shared memory exceeds %zu bytes; use fewer warps", budget);
-  // Rounds are numbered in 27 bits of the stamp marks: split very long runs.
-  const uint64_t max_chunk = (uint64_t)1 << 26;
+  // Rounds are numbered in the upper 26 bits of the stamp marks: split very long runs.
+  const uint64_t max_chunk = (uint64_t)1 << 25;
   if (r->n_trials > max_chunk && r->trace_acc)
     return fail(CEMC_ERR_LIMIT, "traced runs are limited to %llu trials per call", (unsigned long long)max_chunk);
   for (uint64_t done = 0; done < r->n_trials;) {

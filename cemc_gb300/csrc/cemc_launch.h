@@ -11,8 +11,10 @@ namespace cemc {
 
 struct RunArgs {
   int n_chains, warps;
+  int cl;                  // CTAs per chain (1, or 2 for a thread-block cluster pair)
+  int ring_bits;           // log2 of the draw / neighbour-row ring size
   int occ_smem, trk_smem;  // 1: the chain's occupation / swap tracker lives in shared memory
-  int stamp_bits;          // log2 of the conflict-stamp table size
+  int stamp_bits;          // log2 of the size of each of the two conflict-stamp tables
   uint64_t seed, n_trials;
   int8_t *occ;
   double *cf, *energy;
@@ -31,8 +33,12 @@ struct RunArgs {
   uint64_t chunk_offset;  // trials of this chain already run by earlier chunks of the same call
 };
 
-constexpr int kRing = 128;     // trial slots of the draw / row ring (power of two, > 3 * kMaxEval)
-constexpr int kMaxEval = 31;   // trial-evaluating warps; one more warp is the helper
+constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two more warps are helpers
+constexpr int kRoundSlots = 64;  // trial records per round: up to 2 CTAs x 30 warps
+constexpr int kPrefetchRounds = 3;  // the helper draws this many rounds of trials ahead
+
+// Ring size (log2) for `cl` CTAs per chain: holds kPrefetchRounds rounds of trials.
+__host__ __device__ inline int ring_bits_for(int cl) { return cl == 2 ? 8 : 7; }
 
 // Per-trial draw, written by the helper warp: site (flips), Philox words.
 struct Draw {
@@ -43,7 +49,9 @@ struct Draw {
 struct McLayout {
   size_t cf, eci, w, acc, cfw, coef, bf, terms, lane_term, kind, misc;
   size_t sp_eci, sp_masks, sp_shift, sp_lane;  // spin-basis tables (empty unless n_cl > 0)
-  size_t rec, rec_stride, rec_tsa, rec_tsb, rec_acc, rec_der, rec_de, rec_d;
+  // per-round trial records (two buffers, by round parity), kRoundSlots entries each
+  size_t rec, rec_stride, rec_sa, rec_sb, rec_de, rec_ds, rec_acc, rec_la, rec_lb, rec_A, rec_B;
+  size_t drow;  // [warps][n_eci] correlation-function changes of each warp's own trial
   size_t draws, rows;
   size_t warp0, warp_stride, warp_part;
   size_t occ, trk, stamp;
@@ -53,12 +61,14 @@ struct McLayout {
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// Shared-memory carve-up of mc_kernel for `warps` evaluating warps.
+// Shared-memory carve-up of mc_kernel for `warps` evaluating warps per CTA.
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
-                                              int trk_smem, int stamp_bits, int n_cl = 0, int n_masks = 0) {
+                                              int trk_smem, int stamp_bits, int n_cl, int n_masks, int ring_bits,
+                                              bool spin) {
   McLayout L;
   size_t o = 0;
   const size_t K = (size_t)g.n_eci;
+  const size_t S = kRoundSlots;
   L.cf = o;
   o = align16(o + 8 * K);
   L.eci = o;
@@ -89,28 +99,43 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + (size_t)n_masks);
   L.sp_lane = o;
   if (n_cl > 0) o = align16(o + 4 * (33 + 32));
-  // two buffers of per-trial records (current round / round being booked)
-  L.rec_tsa = 0;
-  L.rec_tsb = 4 * 32;
-  L.rec_acc = 8 * 32;
-  L.rec_der = align16(L.rec_acc + 32);
-  L.rec_de = L.rec_der;  // unused
-  L.rec_d = align16(L.rec_der + (size_t)rsize * 32);
-  L.rec_stride = align16(L.rec_d + (size_t)rsize * 32 * K);
+  size_t r = 0;
+  L.rec_sa = r;
+  r += 4 * S;
+  L.rec_sb = r;
+  r += 4 * S;
+  L.rec_la = r;
+  r += 4 * S;
+  L.rec_lb = r;
+  r += 4 * S;
+  L.rec_de = r;
+  r += (size_t)rsize * S;
+  L.rec_ds = r;
+  r += (size_t)rsize * S * CEMC_MAX_BF;
+  L.rec_acc = r;
+  r += S;
+  L.rec_A = r;
+  r += S;
+  L.rec_B = r;
+  r += S;
+  L.rec_stride = align16(r);
   L.rec = o;
   o = align16(o + 2 * L.rec_stride);
+  L.drow = o;
+  o = align16(o + (size_t)rsize * warps * K);
+  const size_t ring = (size_t)1 << ring_bits;
   L.draws = o;
-  o = align16(o + sizeof(Draw) * (size_t)kRing);
+  o = align16(o + sizeof(Draw) * ring);
   L.rows = o;
-  if (move == CEMC_MOVE_FLIP) o = align16(o + 4 * (size_t)kRing * g.cpad);
+  if (move == CEMC_MOVE_FLIP) o = align16(o + 4 * ring * g.cpad);
   const size_t vals = (size_t)rsize * g.vals_len * (move == CEMC_MOVE_SWAP ? 2 : 1);
   L.warp_part = align16(vals);
-  L.warp_stride = align16(L.warp_part + (size_t)rsize * g.n_slots * 32);
+  L.warp_stride = spin ? 0 : align16(L.warp_part + (size_t)rsize * g.n_slots * 32);
   L.warp0 = o;
   o = align16(o + L.warp_stride * (size_t)warps);
   L.stamp_bits = stamp_bits;
   L.stamp = o;
-  o = align16(o + 4 * ((size_t)1 << stamp_bits));
+  o = align16(o + 2 * 4 * ((size_t)1 << stamp_bits));
   L.occ = o;
   if (occ_smem) o = align16(o + (size_t)g.n_sites);
   L.trk = o;
@@ -122,5 +147,7 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
 struct SpinDev;
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       const SpinDev *spin);
+// Clusters of `cl` CTAs (each with `smem` bytes) that can be resident at once; 0 if none.
+int max_active_clusters(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, bool spin);
 
 }  // namespace cemc

@@ -7,32 +7,47 @@
 // cpp/src/ce_updater.cpp:313-555) by one launch that runs many trials of many
 // chains.
 //
-// One CTA owns one chain for the whole launch; the chain's occupation (int8
-// species ids) sits in shared memory when it fits.  A chain is a sequential
-// Markov chain, so parallelism inside it comes from speculation.  Each round,
-// evaluating warp w computes trial t0 + w against the state at the start of
-// the round.  A trial's energy change depends only on the species of its own
-// sites and of their neighbour columns, so it stays valid unless an earlier
-// ACCEPTED trial of the same round changed one of those sites.  Accepted
-// trials stamp their site and its neighbourhood in a shared-memory table with
-// (round, trial) marks; warp 0 then reads one stamp per trial, commits the
-// longest prefix with no earlier conflicting accept (exactly what sequential
-// Metropolis over the same stream does) and the first conflicting trial is
-// re-evaluated next round.  When the stamp table is smaller than the
-// supercell it is indexed by site & mask: an alias can only report a false
-// conflict, which shortens the committed prefix and never changes a result.
-// The neighbour relation is symmetric (checked when the geometry is built),
-// so "accepted site in my neighbourhood" equals "my site in its neighbourhood".
+// A chain is owned by one CTA, or by a pair of CTAs on two SMs (a
+// thread-block cluster of two).  Each CTA keeps a full copy of the chain's
+// occupation (int8 species ids) in shared memory when it fits.  A chain is a
+// sequential Markov chain, so parallelism inside it comes from speculation:
+// each round evaluates trials t0 .. t0 + CW - 1 (CW = CTAs x evaluating warps)
+// against the state at the start of the round, one trial per warp.  A trial's
+// energy change depends only on the species of its own sites and of their
+// neighbour columns, so it stays valid unless an earlier ACCEPTED trial of the
+// same round changed one of those sites.  Accepted trials stamp their site
+// and its neighbourhood with (round, trial) marks into a shared-memory table
+// (both CTAs' tables in a pair); after the round barrier every warp reads one
+// stamp per trial, finds the longest prefix with no earlier conflicting
+// accept (exactly what sequential Metropolis over the same stream does) and
+// applies all of its accepted moves itself.  These stores are idempotent
+// (committed moves touch disjoint sites, and a swap's list positions are
+// recorded with the trial), so no second barrier is needed before the next
+// round reads the occupation; stamp tables and trial records alternate by
+// round parity, so the next round's writes never meet this round's reads.
+// The first conflicting trial is re-evaluated next round.  When a stamp table
+// is smaller than the supercell it is indexed by site & mask: an alias can
+// only report a false conflict, which shortens the committed prefix and never
+// changes a result.  The neighbour relation is symmetric (checked when the
+// geometry is built), so "accepted site in my neighbourhood" equals "my site
+// in its neighbourhood".
 //
-// One extra helper warp runs off the critical path: it precomputes the
-// counter-based draws (philox.h) of upcoming trials, prefetches their
-// neighbour-table rows from L2/HBM into a shared-memory ring with cp.async two
-// rounds ahead (single-site flips, whose site does not depend on the state),
-// and folds the previous round's records (double-buffered) into per-lane
-// running sums of energy and singlets.  Each evaluating warp adds the
-// correlation-function changes of its own committed accepted trials to
-// per-warp sums; the correlation functions and the energy are brought up to
-// date in FP64 once, at the end of the launch.
+// In a pair, each CTA writes its trial records and stamps into both CTAs'
+// shared memory (distributed shared memory stores and reductions), so every
+// warp of both CTAs reads the same data after the cluster barrier and
+// computes the same committed prefix.  Both CTAs also exchange their round
+// start before each barrier; a mismatch stops both with CEMC_ERR_INTERNAL
+// instead of letting them wait at different barriers.
+//
+// Two extra helper warps per CTA run off the critical path.  The fetcher
+// precomputes the counter-based draws (philox.h) of upcoming trials and
+// prefetches their neighbour-table rows from L2/HBM into a shared-memory ring
+// with cp.async (single-site flips, whose site does not depend on the state).
+// The booker folds the previous round's records into per-lane running sums of
+// energy and singlets (in a pair, CTA q takes trials 32q .. 32q + 31 of each
+// round and carries the other half's totals).  Each evaluating warp adds the correlation-function changes of its
+// own committed accepted trials to per-warp sums; correlation functions and
+// energy are brought up to date in FP64 once, at the end of the launch.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -105,23 +120,72 @@ __device__ __forceinline__ uint32_t spin_lane_parities(const uint2 *masks, const
   return packed;
 }
 
-// Number of odd-parity multi-site terms of cluster ECI k over the warp.
-__device__ __forceinline__ int spin_odd(uint32_t packed, int k, int first) {
-  const int sl = k - first;
-  const int v = (sl >= 0 && sl < 5) ? (int)((packed >> (6 * sl)) & 63u) : 0;
-  return __reduce_add_sync(kFull, v);
+
+
+// ---- thread-block cluster pairs ---------------------------------------------
+__device__ __forceinline__ unsigned cluster_cta_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+// Every thread of both CTAs; release / acquire orders the shared-memory
+// stores (local and remote) made before it against the reads after it.
+__device__ __forceinline__ void cluster_barrier() {
+  __syncwarp();  // the .aligned forms want every lane of the warp at the same instruction
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t peer_addr(const void *p, unsigned rank) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_peer(uint32_t a, int32_t v) {
+  asm volatile("st.shared::cluster.s32 [%0], %1;\n" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_peer(uint32_t a, int8_t v) {
+  asm volatile("st.shared::cluster.s8 [%0], %1;\n" ::"r"(a), "r"((int)v) : "memory");
+}
+__device__ __forceinline__ void st_peer(uint32_t a, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;\n" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_peer(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;\n" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_peer(uint32_t a, uint64_t v) {
+  asm volatile("st.shared::cluster.u64 [%0], %1;\n" ::"r"(a), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_max_peer(uint32_t a, uint32_t v) {
+  asm volatile("red.shared::cluster.max.u32 [%0], %1;\n" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ double ld_peer_acc(const double *p, unsigned rank) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(peer_addr(p, rank)) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
+  float hi, lo;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(hi), "=f"(lo) : "r"(peer_addr(p, rank)) : "memory");
+  return (double)hi + (double)lo;
 }
 
-template <typename R, int MOVE, bool SPIN>
+template <typename R, int MOVE, bool SPIN, int CL>
 __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
-  const int W = a.warps;  // evaluating warps; warp W is the helper
+  const int W = a.warps;  // evaluating warps per CTA; warps W (booker) and W + 1 (fetcher) are helpers
+  const int CW = CL * W;  // trials per round
   const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits, SPIN ? sd.n_cl : 0,
-                               SPIN ? sd.n_masks : 0);
-  const int chain = blockIdx.x;
+                               SPIN ? sd.n_masks : 0, a.ring_bits, SPIN);
+  const uint32_t rmask = (1u << a.ring_bits) - 1u;
+  const int rank = (CL == 2) ? (int)cluster_cta_rank() : 0;
+  const unsigned peer = (unsigned)(rank ^ 1);
+  const int chain = blockIdx.x / CL;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool helper = (warp == W);
+  const bool helper = (warp >= W);
+  const bool booker = (warp == W), fetcher = (warp == W + 1);
+  const int gidx = rank * W + warp;  // this warp's trial slot in a round
   const int N = g.n_sites, n_eci = g.n_eci, cpad = g.cpad;
   const uint32_t hmask = (1u << L.stamp_bits) - 1u;
 
@@ -129,10 +193,11 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   double *eci_s = reinterpret_cast<double *>(smem + L.eci);
   double *w_s = reinterpret_cast<double *>(smem + L.w);
   // Running sums of this launch, FP64 in FP64 mode and double-float in FP32
-  // mode.  The thermodynamic sums are kept per lane of the helper warp (lane =
-  // position of a trial in its round) and the committed correlation-function
-  // changes per evaluating warp, so no round needs a cross-lane or cross-warp
-  // reduction of them; both are reduced once, in fixed order, in the epilogue.
+  // mode.  The thermodynamic sums are kept per lane of the booker warps
+  // (lane j of CTA q takes trial 32q + j of each round) and the committed
+  // correlation-function changes per evaluating warp, so no round needs a
+  // cross-lane or cross-warp reduction of them; both are reduced once, in
+  // fixed order, in the epilogue.
   constexpr bool DF = (sizeof(R) == 4);
   using A = typename std::conditional<DF, df64, double>::type;
   constexpr int NACC = 2 + 3 * CEMC_MAX_BF;
@@ -148,13 +213,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int32_t *eci_lane_s = first_s + 32;
   int8_t *kind_s = reinterpret_cast<int8_t *>(smem + L.kind);
   int8_t *dec_s = kind_s + n_eci;
-  // misc: [0] committed count, [1] status, [2] species present, [4..12) present ids,
-  //       [12..20) site-list starts, [20..28) site-list counts
+  // misc: [1] status, [2] species present, [4..12) present ids, [12..20) site-list
+  //       starts, [20..28) site-list counts, [32..36) round starts written by the peer CTA,
+  //       [36..38) accept count of this CTA's booker
   int32_t *misc = reinterpret_cast<int32_t *>(smem + L.misc);
+  uint64_t *t0_slot = reinterpret_cast<uint64_t *>(misc + 32);
+  uint64_t *nacc_slot = reinterpret_cast<uint64_t *>(misc + 36);  // the booker's accept count (pairs)
   Draw *draws = reinterpret_cast<Draw *>(smem + L.draws);
   int32_t *rows = reinterpret_cast<int32_t *>(smem + L.rows);
-  uint32_t *stamp = reinterpret_cast<uint32_t *>(smem + L.stamp);
+  uint32_t *stamp = reinterpret_cast<uint32_t *>(smem + L.stamp);  // two tables of hmask + 1 entries
   unsigned char *rec0 = smem + L.rec;
+  R *drow = reinterpret_cast<R *>(smem + L.drow);
   unsigned char *wbase = smem + L.warp0 + (size_t)(helper ? 0 : warp) * L.warp_stride;
   R *va = reinterpret_cast<R *>(wbase);
   R *vb = va + g.vals_len;
@@ -178,7 +247,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   for (int k = tid; k < n_eci; k += blockDim.x) {
     const int kind = g.eci_kind[k];
     const double e = a.eci[(size_t)chain * n_eci + k];
-    cf_s[k] =a.cf[(size_t)chain * n_eci + k];
+    cf_s[k] = a.cf[(size_t)chain * n_eci + k];
     eci_s[k] = e;
     w_s[k] = (kind == 2) ? g.eci_w[k] : 0.0;
     coef_s[k] = (R)(kind == 2 ? e * (double)N * g.eci_w[k] : (kind == 1 ? e : 0.0));
@@ -195,17 +264,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     uint2 *dst = reinterpret_cast<uint2 *>(terms_s);
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
-  for (uint32_t i = tid; i <= hmask; i += blockDim.x) stamp[i] = 0u;
-  for (int i = tid; i < W * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
-  for (int i = tid; i < NACC * 32; i += blockDim.x) lacc[i] = acc_from<A>(0.0);
-  {
-    // zero the change rows of both record buffers (the spin path writes only
-    // the entries of cluster and singlet ECIs)
-    for (int i = tid; i < 2 * 32 * n_eci; i += blockDim.x) {
-      const int buf = i / (32 * n_eci), j = i - buf * 32 * n_eci;
-      reinterpret_cast<R *>(rec0 + (size_t)buf * L.rec_stride + L.rec_d)[j] = (R)0;
-    }
+  for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
+  for (int i = tid; i < W * n_eci; i += blockDim.x) {
+    cfw[i] = acc_from<A>(0.0);
+    drow[i] = (R)0;  // the spin path writes only the entries of cluster and singlet ECIs
   }
+  for (int i = tid; i < NACC * 32; i += blockDim.x) lacc[i] = acc_from<A>(0.0);
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
     for (int t = tid; t < sd.n_masks; t += blockDim.x) {
@@ -228,6 +292,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
   if (tid == 0) {
     misc[1] = 0;
+    t0_slot[0] = t0_slot[1] = 0;
     if (SWAP) {
       int np = 0;
       for (int s = 0; s < g.n_sym; ++s) {
@@ -240,7 +305,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       if (np < 2) misc[1] = CEMC_ERR_STATE;
     }
     for (int b = 0; b < CEMC_MAX_BF; ++b)
-      s_start[b] = acc_from<A>(b < g.n_bf ? a.cf[(size_t)chain * n_eci + g.singlet_eci[b]] : 0.0);
+      s_start[b] = acc_from<A>((b < g.n_bf && g.singlet_eci[b] >= 0) ? a.cf[(size_t)chain * n_eci + g.singlet_eci[b]]
+                                                                     : 0.0);
     s_start[CEMC_MAX_BF] = acc_from<A>(1.0 / (double)N);
   }
 
@@ -258,8 +324,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   const int acc_row = a.accum_slot ? a.accum_slot[chain] : chain;
   const double e_ref = a.accum ? a.accum[acc_row].e_ref : 0.0;
 
-  // Helper-warp state: energy relative to e_ref and, per singlet, the launch's
-  // summed singlet changes (the singlet after a trial is start + sum / N).
+  // Helper-warp state (CTA 0): energy relative to e_ref and, per singlet, the
+  // launch's summed singlet changes (the singlet after a trial is start + sum / N).
   A eoff = acc_from<A>(a.energy[chain] - e_ref);
   A dsum[NBF];
 #pragma unroll
@@ -267,12 +333,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   uint64_t n_acc_launch = 0;
   uint64_t fill_end = t_first;
 
-  // Draws (and, for flips, neighbour rows) of trials [fill_end, min(t0 + 3W, t_end)).
+  // Draws (and, for flips, neighbour rows) of trials [fill_end, min(t0 + 3 CW, t_end)).
   auto prefetch = [&](uint64_t t0) {
-    uint64_t want = t0 + 3 * (uint64_t)W;
+    uint64_t want = t0 + (uint64_t)kPrefetchRounds * (uint64_t)CW;
     if (want > t_end) want = t_end;
     for (uint64_t t = fill_end + lane; t < want; t += 32) {
-      const int slot = (int)(t & (kRing - 1));
+      const uint32_t slot = (uint32_t)t & rmask;
       const cemc_u32x4 w0 = cemc_trial_draw(a.seed, key, t, 0);
       Draw d;
       d.w0 = w0.v[0];
@@ -298,23 +364,24 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     cp_async_commit();
   };
 
-  // Fold round records (buffer `rec`, `ks` committed trials) into the running
-  // sums.  Lane j handles trial j of the round: one inclusive scan gives the
-  // energy and singlet offsets after each trial, and each lane adds its own
-  // values to its own sums; a round without accepted trials needs no scan.
-  auto book = [&](const unsigned char *rec, int ks) {
-    const int8_t *tacc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
-    const R *tder = reinterpret_cast<const R *>(rec + L.rec_der);
-    const R *tD = reinterpret_cast<const R *>(rec + L.rec_d);
-    const bool mine = lane < ks;
-    const bool acc = mine && tacc[lane];
+  // Fold trials [off, off + kh) of round records `rec` into the running sums.
+  // Lane j takes trial off + j: one inclusive scan gives the energy and singlet
+  // offsets after each trial, and each lane adds its own values to its own
+  // sums; a half without accepted trials needs no scan.
+  auto book_half = [&](const unsigned char *rec, int off, int kh) {
+    const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
+    const R *r_de = reinterpret_cast<const R *>(rec + L.rec_de);
+    const R *r_ds = reinterpret_cast<const R *>(rec + L.rec_ds);
+    const int gg = off + lane;
+    const bool mine = lane < kh;
+    const bool acc = mine && r_acc[gg];
     const unsigned am = __ballot_sync(kFull, acc);
     n_acc_launch += (uint64_t)__popc(am);
     if (!a.accum) return;
-    R x = acc ? tder[lane] : (R)0;
+    R x = acc ? r_de[gg] : (R)0;
     R ds[NBF];
 #pragma unroll
-    for (int b = 0; b < NBF; ++b) ds[b] = (acc && b < g.n_bf) ? tD[(size_t)lane * n_eci + g.singlet_eci[b]] : (R)0;
+    for (int b = 0; b < NBF; ++b) ds[b] = (acc && b < g.n_bf) ? r_ds[b * kRoundSlots + gg] : (R)0;
     if (am) {
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -345,18 +412,52 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       }
     }
     if (am) {
-      eoff = acc_add_x(eoff, __shfl_sync(kFull, x, ks - 1));
+      eoff = acc_add_x(eoff, __shfl_sync(kFull, x, kh - 1));
 #pragma unroll
-      for (int b = 0; b < NBF; ++b) dsum[b] = acc_add_x(dsum[b], __shfl_sync(kFull, ds[b], ks - 1));
+      for (int b = 0; b < NBF; ++b) dsum[b] = acc_add_x(dsum[b], __shfl_sync(kFull, ds[b], kh - 1));
+    }
+  };
+  // Totals of trials [off, off + kh) added to the running offsets only (the
+  // other CTA of a pair books those trials).
+  auto carry_half = [&](const unsigned char *rec, int off, int kh) {
+    if (!a.accum) return;
+    const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
+    const R *r_de = reinterpret_cast<const R *>(rec + L.rec_de);
+    const R *r_ds = reinterpret_cast<const R *>(rec + L.rec_ds);
+    const int gg = off + lane;
+    const bool acc = lane < kh && r_acc[gg];
+    if (!__ballot_sync(kFull, acc)) return;
+    eoff = acc_add_x(eoff, warp_sum(acc ? r_de[gg] : (R)0));
+#pragma unroll
+    for (int b = 0; b < NBF; ++b)
+      if (b < g.n_bf) dsum[b] = acc_add_x(dsum[b], warp_sum(acc ? r_ds[b * kRoundSlots + gg] : (R)0));
+  };
+  auto book = [&](const unsigned char *rec, int ks) {
+    const int k0 = ks < 32 ? ks : 32, k1 = ks - k0;
+    if (rank == 0) {
+      book_half(rec, 0, k0);
+      if (k1 > 0) carry_half(rec, 32, k1);
+    } else {
+      carry_half(rec, 0, k0);
+      if (k1 > 0) book_half(rec, 32, k1);
     }
   };
 
-  __syncthreads();
-  if (misc[1] != 0) {
-    if (tid == 0 && a.status) a.status[chain] = misc[1];
+  // Store into this CTA's shared memory and, in a pair, the peer's copy.
+  auto put = [&](auto *p, auto v) {
+    *p = v;
+    if (CL == 2) st_peer(peer_addr(p, peer), v);
+  };
+
+  if (CL == 2)
+    cluster_barrier();  // the peer's tables are initialised before any remote store
+  else
+    __syncthreads();
+  if (misc[1] != 0) {  // same verdict in both CTAs of a pair: it depends on the chain's inputs only
+    if (tid == 0 && rank == 0 && a.status) a.status[chain] = misc[1];
     return;
   }
-  if (helper) {
+  if (fetcher) {
     prefetch(t_first);
     cp_async_wait_all();
   }
@@ -367,30 +468,42 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   SpinEci sp_e{};
   R sp_coef = (R)0;
   unsigned sp_multi = 0;  // cluster ECIs with multi-site terms
+  int sp_tlo = 0, sp_thi = 0, sp_first = 0;  // this lane's range of multi-site terms
   if (SPIN) {
+    sp_tlo = sp_lane_term[lane];
+    sp_thi = sp_lane_term[lane + 1];
+    sp_first = sp_lane_first[lane];
     if (lane < sd.n_cl) {
       sp_e = sp_eci[lane];
       sp_coef = coef_s[sp_e.eci];
     }
     sp_multi = __ballot_sync(kFull, lane < sd.n_cl && sp_e.n_multi > 0);
   }
+
   uint64_t t0 = t_first;
   uint32_t round = 1;
   int ks_prev = 0;
-  while (t0 < t_end) {
+  while (true) {
+    const bool active = t0 < t_end;
     unsigned char *rec = rec0 + (size_t)(round & 1) * L.rec_stride;
-    int32_t *tsa = reinterpret_cast<int32_t *>(rec + L.rec_tsa);
-    int32_t *tsb = reinterpret_cast<int32_t *>(rec + L.rec_tsb);
-    int8_t *tacc = reinterpret_cast<int8_t *>(rec + L.rec_acc);
-    R *tder = reinterpret_cast<R *>(rec + L.rec_der);
-    R *tD = reinterpret_cast<R *>(rec + L.rec_d);
+    int32_t *r_sa = reinterpret_cast<int32_t *>(rec + L.rec_sa);
+    int32_t *r_sb = reinterpret_cast<int32_t *>(rec + L.rec_sb);
+    int32_t *r_la = reinterpret_cast<int32_t *>(rec + L.rec_la);
+    int32_t *r_lb = reinterpret_cast<int32_t *>(rec + L.rec_lb);
+    int8_t *r_acc = reinterpret_cast<int8_t *>(rec + L.rec_acc);
+    int8_t *r_A = reinterpret_cast<int8_t *>(rec + L.rec_A);
+    int8_t *r_B = reinterpret_cast<int8_t *>(rec + L.rec_B);
+    R *r_de = reinterpret_cast<R *>(rec + L.rec_de);
+    R *r_ds = reinterpret_cast<R *>(rec + L.rec_ds);
+    uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
+    R *Dw = drow + (size_t)(helper ? 0 : warp) * n_eci;
     if (!helper) {
       // ---- phase A: every evaluating warp computes one trial speculatively ----
-      const uint64_t t = t0 + (uint64_t)warp;
-      if (t < t_end) {
-        const int slot = (int)(t & (kRing - 1));
+      const uint64_t t = t0 + (uint64_t)gidx;
+      if (active && t < t_end) {
+        const uint32_t slot = (uint32_t)t & rmask;
         const Draw dr = draws[slot];
-        int sa, sb = -1, na;
+        int sa, sb = -1, na, A_ = 0, B_ = 0;
         int nbra[4], nbrb[4] = {-1, -1, -1, -1};
         uint32_t ua, ub;
         uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
@@ -411,39 +524,40 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
           int ib = (int)cemc_below(dr.w1, (uint32_t)(n_present - 1));
           ib += (ib >= ia);
-          const int A = misc[4 + ia], B = misc[4 + ib];
-          sa = trk[misc[12 + A] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A])];
-          sb = trk[misc[12 + B] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B])];
-          na = B;
+          A_ = misc[4 + ia];
+          B_ = misc[4 + ib];
+          sa = trk[misc[12 + A_] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A_])];
+          sb = trk[misc[12 + B_] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B_])];
+          na = B_;
           ua = dr.x0;
           ub = dr.x1;
           // first half: site a takes B; second half: site b takes A with a already changed
           if (!SPIN) {
-            gather_vals<R>(g, occ, bf_s, sa, A, B, -1, 0, va, nbra, lane);
-            gather_vals<R>(g, occ, bf_s, sb, B, A, sa, B, vb, nbrb, lane);
+            gather_vals<R>(g, occ, bf_s, sa, A_, B_, -1, 0, va, nbra, lane);
+            gather_vals<R>(g, occ, bf_s, sb, B_, A_, sa, B_, vb, nbrb, lane);
           } else {
-            occ_a_bit = (uint32_t)A ^ xorv;
+            occ_a_bit = (uint32_t)A_ ^ xorv;
             spin_ballot(g, occ, g.table + (size_t)sa * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
             spin_ballot(g, occ, g.table + (size_t)sb * cpad, xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
           }
         }
         R de;
+        int delta = 0;
         if (!SPIN) {
           __syncwarp();
           lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
           __syncwarp();
-          de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb,
-                                    tD + (size_t)warp * n_eci, lane);
+          de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb, Dw, lane);
+          __syncwarp();
         } else {
           // P_k = sum over the terms of cluster ECI k of the product of the other
           // members' spins; D_k = delta * P_k with delta = -2 s_a the spin change.
           // Lane k evaluates cluster ECI k: its pair terms by popcounts of its shell
           // masks, its multi-site terms from one warp reduction per ECI that has any.
-          R *Dw = tD + (size_t)warp * n_eci;
-          const int delta = ((occ_a_bit) ? 2 : -2);
-          const int t_lo = sp_lane_term[lane], t_hi = sp_lane_term[lane + 1], first = sp_lane_first[lane];
-          const uint32_t pa = spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wa_lo, wa_hi);
-          const uint32_t pb = SWAP ? spin_lane_parities(sp_masks, sp_shift, t_lo, t_hi, wb_lo, wb_hi) : 0u;
+          delta = ((occ_a_bit) ? 2 : -2);
+          const int first = sp_first;
+          const uint32_t pa = spin_lane_parities(sp_masks, sp_shift, sp_tlo, sp_thi, wa_lo, wa_hi);
+          const uint32_t pb = SWAP ? spin_lane_parities(sp_masks, sp_shift, sp_tlo, sp_thi, wb_lo, wb_hi) : 0u;
           int my_odd = 0;
           for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
             const int k = __ffs(mm) - 1;
@@ -475,95 +589,170 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         int acc = 0;
         if (lane == 0) {
           acc = metropolis<R>(de, ua, ub, kT, inv_kT);
-          tsa[warp] = sa;
-          tsb[warp] = SWAP ? sb : na;
-          tacc[warp] = (int8_t)acc;
-          tder[warp] = de;
+          put(&r_sa[gidx], (int32_t)sa);
+          put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
+          put(&r_acc[gidx], (int8_t)acc);
+          put(&r_de[gidx], de);
+          for (int b = 0; b < g.n_bf; ++b) {
+            R v = (R)0;
+            if (SPIN)
+              v = (R)(SWAP ? 0 : delta);
+            else if (g.singlet_eci[b] >= 0)
+              v = Dw[g.singlet_eci[b]];
+            put(&r_ds[b * kRoundSlots + gidx], v);
+          }
+          if (SWAP) {
+            put(&r_la[gidx], (int32_t)loc[sa]);
+            put(&r_lb[gidx], (int32_t)loc[sb]);
+            put(&r_A[gidx], (int8_t)A_);
+            put(&r_B[gidx], (int8_t)B_);
+          }
         }
         acc = __shfl_sync(kFull, acc, 0);
         if (acc) {
-          const uint32_t mark = (round << 5) | (uint32_t)(31 - warp);
+          const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            if (nbra[q] >= 0) atomicMax(&stamp[(uint32_t)nbra[q] & hmask], mark);
-            if (SWAP && nbrb[q] >= 0) atomicMax(&stamp[(uint32_t)nbrb[q] & hmask], mark);
+            if (nbra[q] >= 0) {
+              uint32_t *p = &tab[(uint32_t)nbra[q] & hmask];
+              atomicMax(p, mark);
+              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+            }
+            if (SWAP && nbrb[q] >= 0) {
+              uint32_t *p = &tab[(uint32_t)nbrb[q] & hmask];
+              atomicMax(p, mark);
+              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+            }
           }
           if (lane == 0) {
-            atomicMax(&stamp[(uint32_t)sa & hmask], mark);
-            if (SWAP) atomicMax(&stamp[(uint32_t)sb & hmask], mark);
+            uint32_t *p = &tab[(uint32_t)sa & hmask];
+            atomicMax(p, mark);
+            if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+            if (SWAP) {
+              p = &tab[(uint32_t)sb & hmask];
+              atomicMax(p, mark);
+              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+            }
           }
         }
       }
-    } else {
-      // ---- helper: book the previous round, then draw / prefetch ahead ----------
+    } else if (booker) {
+      // ---- helpers: book the previous round; draw / prefetch ahead ----------------
       if (round > 1) book(rec0 + (size_t)((round - 1) & 1) * L.rec_stride, ks_prev);
-      prefetch(t0);
+    } else {
+      if (active) prefetch(t0);
       cp_async_wait_prev();
     }
-    __syncthreads();
-
-    if (!helper) {
-      // ---- phase B: every warp finds the first trial invalidated by an earlier
-      // accept (the committed prefix) and commits its own trial if inside it.
-      const int nv = (t_end - t0) < (uint64_t)W ? (int)(t_end - t0) : W;
-      bool conflict = false;
-      if (lane < nv) {
-        const uint32_t v = stamp[(uint32_t)tsa[lane] & hmask];
-        conflict = ((v >> 5) == round) && ((31u - (v & 31u)) < (uint32_t)lane);
-        if (SWAP) {
-          const uint32_t v2 = stamp[(uint32_t)tsb[lane] & hmask];
-          conflict |= ((v2 >> 5) == round) && ((31u - (v2 & 31u)) < (uint32_t)lane);
-        }
+    if (CL == 2) {
+      if (tid == 0) st_peer(peer_addr(&t0_slot[round & 1], peer), t0);
+      cluster_barrier();
+      if (t0_slot[round & 1] != t0) {  // both CTAs see the same mismatch and stop together
+        if (tid == 0) misc[1] = CEMC_ERR_INTERNAL;
+        break;
       }
-      const unsigned cm = __ballot_sync(kFull, conflict);
-      const int ks = cm ? (__ffs(cm) - 1) : nv;
-      if (lane == 0 && warp < ks) {
-        const int sa = tsa[warp];
-        if (tacc[warp]) {
+    } else {
+      __syncthreads();
+    }
+    if (!active) break;
+
+    // ---- phase B (every warp): the committed prefix, then its accepted moves ----
+    const int nv = (t_end - t0) < (uint64_t)CW ? (int)(t_end - t0) : CW;
+    auto conflicted = [&](int gg) {
+      const uint32_t v = tab[(uint32_t)r_sa[gg] & hmask];
+      bool c = ((v >> 6) == round) && ((uint32_t)(63 - (v & 63u)) < (uint32_t)gg);
+      if (SWAP) {
+        const uint32_t v2 = tab[(uint32_t)r_sb[gg] & hmask];
+        c |= ((v2 >> 6) == round) && ((uint32_t)(63 - (v2 & 63u)) < (uint32_t)gg);
+      }
+      return c;
+    };
+    const bool c0 = lane < nv && conflicted(lane);
+    const bool c1 = lane + 32 < nv && conflicted(lane + 32);
+    const unsigned m0 = __ballot_sync(kFull, c0);
+    const unsigned m1 = __ballot_sync(kFull, c1);
+    const int ks = m0 ? (__ffs(m0) - 1) : (m1 ? (31 + __ffs(m1)) : nv);
+    if (!helper) {
+      for (int gg = lane; gg < ks; gg += 32) {
+        if (r_acc[gg]) {
+          const int sa = r_sa[gg];
           if (!SWAP) {
-            occ[sa] = (int8_t)tsb[warp];
+            occ[sa] = (int8_t)r_sb[gg];
           } else {
-            const int sb = tsb[warp];
-            const int A = occ[sa], B = occ[sb];
-            const int la = loc[sa], lb = loc[sb];
-            occ[sa] = (int8_t)B;
-            occ[sb] = (int8_t)A;
-            trk[misc[12 + A] + la] = sb;
+            const int sb = r_sb[gg], A_ = r_A[gg], B_ = r_B[gg], la = r_la[gg], lb = r_lb[gg];
+            occ[sa] = (int8_t)B_;
+            occ[sb] = (int8_t)A_;
+            trk[misc[12 + A_] + la] = sb;
             loc[sb] = la;
-            trk[misc[12 + B] + lb] = sa;
+            trk[misc[12 + B_] + lb] = sa;
             loc[sa] = lb;
           }
         }
-        if (a.trace_acc) {
-          const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + warp - t_first);
-          a.trace_site[2 * idx] = sa;
-          a.trace_site[2 * idx + 1] = tsb[warp];
-          a.trace_acc[idx] = tacc[warp];
-          a.trace_de[idx] = (double)tder[warp];
+      }
+      __syncwarp();
+      if (gidx < ks) {
+        if (r_acc[gidx]) {
+          // this warp's committed accepted trial: add its change row to the warp's sums
+          A *cw = cfw + (size_t)warp * n_eci;
+          for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], Dw[k]);
+        }
+        if (a.trace_acc && lane == 0) {
+          const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + gidx - t_first);
+          a.trace_site[2 * idx] = r_sa[gidx];
+          a.trace_site[2 * idx + 1] = r_sb[gidx];
+          a.trace_acc[idx] = r_acc[gidx];
+          a.trace_de[idx] = (double)r_de[gidx];
         }
       }
-      if (warp < ks && tacc[warp]) {
-        // this warp's committed accepted trial: add its change row to the warp's sums
-        const R *Dw = tD + (size_t)warp * n_eci;
-        A *cw = cfw + (size_t)warp * n_eci;
-        for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], Dw[k]);
-      }
-      if (warp == 0 && lane == 0) misc[0] = ks;
     }
-    __syncthreads();
-    const int ks = misc[0];
-    t0 += (uint64_t)ks;
     ks_prev = ks;
+    t0 += (uint64_t)ks;
     ++round;
   }
 
-  if (helper) {
-    if (round > 1) book(rec0 + (size_t)((round - 1) & 1) * L.rec_stride, ks_prev);
-    cp_async_wait_all();
+  if (fetcher) cp_async_wait_all();
+  if (CL == 2) {
+    if (booker && lane == 0) nacc_slot[0] = n_acc_launch;
+    cluster_barrier();  // the peer's sums are final and readable
+  } else {
+    __syncthreads();
   }
-  __syncthreads();
 
-  // ---- epilogue: write the chain's state back ----------------------------------
+  // ---- epilogue --------------------------------------------------------------
+  const bool ok = misc[1] == 0;
+  double sum_v = 0.0;         // thread tid < NACC: running sum `tid` over the bookers' lanes
+  uint64_t n_acc_total = 0;   // CTA 0's booker: accepted trials of the launch
+  if (rank == 0 && ok) {
+    // the launch's correlation-function changes: per-warp sums of both CTAs in
+    // warp order (exact for integer-valued changes), then one scaling per ECI
+    for (int k = tid; k < n_eci; k += blockDim.x) {
+      const int kind = kind_s[k];
+      double d = 0.0;
+      for (int w = 0; w < W; ++w) d += acc_to(cfw[(size_t)w * n_eci + k]);
+      if (CL == 2)
+        for (int w = 0; w < W; ++w) d += ld_peer_acc(&cfw[(size_t)w * n_eci + k], peer);
+      if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
+      else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
+    }
+    if (a.accum && tid < NACC) {
+      for (int l = 0; l < 32; ++l) sum_v += acc_to(lacc[tid * 32 + l]);
+      if (CL == 2)
+        for (int l = 0; l < 32; ++l) sum_v += ld_peer_acc(&lacc[tid * 32 + l], peer);
+    }
+    if (booker && lane == 0) {
+      n_acc_total = n_acc_launch;
+      if (CL == 2) {
+        uint64_t v;
+        asm volatile("ld.shared::cluster.u64 %0, [%1];\n" : "=l"(v) : "r"(peer_addr(nacc_slot, peer)) : "memory");
+        n_acc_total += v;
+      }
+    }
+  }
+  if (CL == 2) cluster_barrier();  // CTA 1's shared memory stays alive until CTA 0 has read it
+  if (rank != 0) return;
+  if (!ok) {
+    if (tid == 0 && a.status) a.status[chain] = misc[1];
+    return;
+  }
   if (a.occ_smem) {
     int8_t *dst = a.occ + (size_t)chain * N;
     for (int i = tid; i < N; i += blockDim.x) dst[i] = occ[i];
@@ -575,28 +764,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       sl[i] = loc[i];
     }
   }
-  // apply the launch's correlation-function changes: the per-warp sums in warp
-  // order (exact for integer-valued changes), then one scaling per ECI
-  for (int k = tid; k < n_eci; k += blockDim.x) {
-    const int kind = kind_s[k];
-    double d = 0.0;
-    for (int w = 0; w < W; ++w) d += acc_to(cfw[(size_t)w * n_eci + k]);
-    if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
-    else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
-  }
   __syncthreads();
   for (int k = tid; k < n_eci; k += blockDim.x) a.cf[(size_t)chain * n_eci + k] = cf_s[k];
   if (a.accum && tid < NACC) {
-    // running sum `tid` over the helper's lanes, in lane order
     const int b = tid < 2 ? 0 : (tid - 2) % CEMC_MAX_BF;
     if (tid < 2 || b < g.n_bf) {
-      double v = 0.0;
-      for (int l = 0; l < 32; ++l) v += acc_to(lacc[tid * 32 + l]);
       double *sums = &a.accum[acc_row].sum_e;  // sum_e, sum_e2, sum_s[], sum_s2[], sum_se[] in NACC order
-      sums[tid] += v;
+      sums[tid] += sum_v;
     }
   }
-  if (helper && lane == 0) {
+  if (booker && lane == 0) {
     // energy = N * eci . cf in sorted-name order (ce_updater.cpp:236-242)
     double e = 0.0;
     for (int k = 0; k < n_eci; ++k) e += eci_s[k] * cf_s[k];
@@ -605,35 +782,85 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     if (a.accum) {
       cemc_accum *ac = a.accum + acc_row;
       ac->n_samples += my_trials;
-      ac->n_accept += n_acc_launch;
+      ac->n_accept += n_acc_total;
     }
     if (a.status) a.status[chain] = 0;
   }
 }
 
-template <typename R, int MOVE, bool SPIN>
+template <typename R, int MOVE, bool SPIN, int CL>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
-  auto k = mc_kernel<R, MOVE, SPIN>;
+  auto k = mc_kernel<R, MOVE, SPIN, CL>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<a.n_chains, (a.warps + 1) * 32, smem, st>>>(g, a, sd);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(a.n_chains * CL));
+  cfg.blockDim = dim3((unsigned)((a.warps + 2) * 32));
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (CL == 2) ? 1 : 0;
+  e = cudaLaunchKernelEx(&cfg, k, g, a, sd);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
-template <bool SPIN>
+template <typename R, int MOVE, bool SPIN, int CL>
+static int clusters_t(const RunArgs &a, size_t smem) {
+  auto k = mc_kernel<R, MOVE, SPIN, CL>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(a.n_chains * CL));
+  cfg.blockDim = dim3((unsigned)((a.warps + 2) * 32));
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+template <bool SPIN, int CL>
 static cudaError_t launch_p(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                             const SpinDev &sd) {
   if (precision == CEMC_PREC_F32)
-    return move == CEMC_MOVE_SWAP ? launch_t<float, CEMC_MOVE_SWAP, SPIN>(g, a, smem, st, sd)
-                                  : launch_t<float, CEMC_MOVE_FLIP, SPIN>(g, a, smem, st, sd);
-  return move == CEMC_MOVE_SWAP ? launch_t<double, CEMC_MOVE_SWAP, SPIN>(g, a, smem, st, sd)
-                                : launch_t<double, CEMC_MOVE_FLIP, SPIN>(g, a, smem, st, sd);
+    return move == CEMC_MOVE_SWAP ? launch_t<float, CEMC_MOVE_SWAP, SPIN, CL>(g, a, smem, st, sd)
+                                  : launch_t<float, CEMC_MOVE_FLIP, SPIN, CL>(g, a, smem, st, sd);
+  return move == CEMC_MOVE_SWAP ? launch_t<double, CEMC_MOVE_SWAP, SPIN, CL>(g, a, smem, st, sd)
+                                : launch_t<double, CEMC_MOVE_FLIP, SPIN, CL>(g, a, smem, st, sd);
 }
 
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       const SpinDev *spin) {
-  if (spin) return launch_p<true>(g, a, move, precision, smem, st, *spin);
-  return launch_p<false>(g, a, move, precision, smem, st, SpinDev{});
+  if (a.cl == 2) {
+    if (spin) return launch_p<true, 2>(g, a, move, precision, smem, st, *spin);
+    return launch_p<false, 2>(g, a, move, precision, smem, st, SpinDev{});
+  }
+  if (spin) return launch_p<true, 1>(g, a, move, precision, smem, st, *spin);
+  return launch_p<false, 1>(g, a, move, precision, smem, st, SpinDev{});
+}
+
+int max_active_clusters(const DevGeo &, const RunArgs &a, int move, int precision, size_t smem, bool spin) {
+  const bool f32 = precision == CEMC_PREC_F32, swap = move == CEMC_MOVE_SWAP;
+  if (spin) {
+    if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, true, 2>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, true, 2>(a, smem);
+    return swap ? clusters_t<double, CEMC_MOVE_SWAP, true, 2>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, true, 2>(a, smem);
+  }
+  if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, false, 2>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, false, 2>(a, smem);
+  return swap ? clusters_t<double, CEMC_MOVE_SWAP, false, 2>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, false, 2>(a, smem);
 }
 
 }  // namespace cemc

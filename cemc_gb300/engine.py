@@ -225,10 +225,11 @@ class ChainBatch:
 
     # -- library calls -----------------------------------------------------
     def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
-            chain_trials: Optional[torch.Tensor] = None, kernel: int = 0):
+            chain_trials: Optional[torch.Tensor] = None, kernel: int = 0, cluster: int = 0):
         """Run ``n_trials`` trials on every chain in one launch (``cemc_run``).
 
         ``chain_trials`` (device int64, one per chain, each <= n_trials) gives chains their own counts.
+        ``warps`` evaluating warps per CTA; ``cluster`` CTAs per chain (1, 2, or 0 = chosen by the library).
         """
         tr = None
         if trace:
@@ -241,7 +242,7 @@ class ChainBatch:
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
-                         _ptr(chain_trials), int(kernel))
+                         _ptr(chain_trials), int(kernel), int(cluster))
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         if trace:

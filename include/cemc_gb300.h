@@ -28,6 +28,7 @@ extern "C" {
 #define CEMC_ERR_STATE 4      /* move inconsistent with the current occupation (ce_updater.cpp:530-537) */
 #define CEMC_ERR_LIMIT 5      /* a compiled-in limit was exceeded */
 #define CEMC_ERR_TIMEOUT 6    /* a bounded device wait ran out */
+#define CEMC_ERR_INTERNAL 7   /* a device-side consistency check failed (the chain's state was not written) */
 
 #define CEMC_MAX_BF 4         /* decorations per site (species - 1) */
 #define CEMC_MAX_ECI 128      /* ECIs per cluster expansion */
@@ -109,7 +110,7 @@ typedef struct {
   int32_t n_chains;
   int32_t move;        /* CEMC_MOVE_* */
   int32_t precision;   /* CEMC_PREC_* */
-  int32_t warps;       /* warps per chain (trials evaluated per round); 0 = default */
+  int32_t warps;       /* evaluating warps per CTA (trials per round = warps x CTAs per chain); 0 = default */
   uint64_t seed;
   uint64_t n_trials;   /* trials per chain in this launch */
   int8_t *occ;
@@ -133,6 +134,8 @@ typedef struct {
   const uint64_t *chain_trials; /* [n_chains] trials of each chain in this launch (device, each <= n_trials),
                                    NULL = n_trials for every chain; lets a batch mix jobs with different budgets */
   int32_t kernel;      /* CEMC_KERNEL_*: which implementation runs the trials */
+  int32_t cluster;     /* CTAs per chain: 1, 2 (a thread-block cluster pair on two SMs, twice the trials
+                          per round), or 0 = 2 when every chain's pair fits on the GPU at once, else 1 */
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis kernel when
