@@ -26,6 +26,7 @@ PREC_F32 = 1
 KERNEL_AUTO = 0
 KERNEL_GENERIC = 1
 KERNEL_SPIN = 2
+KERNEL_SPIN_HALFWARP = 3
 MAX_BF = 4
 
 _P = C.c_void_p

@@ -184,6 +184,8 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   std::vector<int> spin_mask_cl;     // cluster-ECI slot of each mask
   std::vector<uint8_t> spin_shift;
   std::vector<int32_t> spin_lane_term(33, 0), spin_lane_first(32, 0);
+  std::vector<int32_t> half_lane_term(17, 0), half_lane_first(16, 0);  // the same terms over 16 lanes
+  std::vector<uint8_t> half_shift;
   int minus_id = -1, singlet_eci = -1;
   bool spin_ok = (B == 1 && S == 2 && C <= CEMC_SPIN_MAX_COLS);
   if (spin_ok) {
@@ -234,6 +236,25 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       }
     }
   }
+  // Half-warp form (two flips per warp): cluster ECIs on lanes 0..15, the
+  // multi-site terms cut into 16 lane ranges with the same 6-bit counters.
+  bool half_ok = spin_ok && spin_eci.size() <= 16;
+  if (half_ok) {
+    const int q = (n_masks + 15) / 16;
+    for (int l = 0; l <= 16; ++l) half_lane_term[l] = std::min(l * q, n_masks);
+    half_shift.assign(std::max(n_masks, 1), 0);
+    for (int l = 0; l < 16 && half_ok; ++l) {
+      const int lo = half_lane_term[l], hi = half_lane_term[l + 1];
+      if (lo >= hi) continue;
+      half_lane_first[l] = spin_mask_cl[lo];
+      for (int t = lo; t < hi; ++t) {
+        const int sl = spin_mask_cl[t] - half_lane_first[l];
+        if (sl > 4 || hi - lo > 63) half_ok = false;
+        half_shift[t] = (uint8_t)(6 * sl);
+      }
+    }
+  }
+  if (half_shift.empty()) half_shift.assign(1, 0);
   if (spin_eci.empty()) spin_eci.push_back(cemc::SpinEci{});
   if (spin_masks.empty()) spin_masks.assign(2, 0u);
   if (spin_shift.empty()) spin_shift.assign(1, 0);
@@ -257,6 +278,9 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {spin_shift.data(), spin_shift.size(), 0},
       {spin_lane_term.data(), 33 * 4, 0},
       {spin_lane_first.data(), 32 * 4, 0},
+      {half_shift.data(), half_shift.size(), 0},
+      {half_lane_term.data(), 17 * 4, 0},
+      {half_lane_first.data(), 16 * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -318,6 +342,10 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   geo->spin.shift = reinterpret_cast<const uint8_t *>(base + parts[15].off);
   geo->spin.lane_term = reinterpret_cast<const int32_t *>(base + parts[16].off);
   geo->spin.lane_first = reinterpret_cast<const int32_t *>(base + parts[17].off);
+  geo->spin.half_ok = half_ok ? 1 : 0;
+  geo->spin.half_shift = reinterpret_cast<const uint8_t *>(base + parts[18].off);
+  geo->spin.half_lane_term = reinterpret_cast<const int32_t *>(base + parts[19].off);
+  geo->spin.half_lane_first = reinterpret_cast<const int32_t *>(base + parts[20].off);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&geo->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -348,8 +376,22 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     return fail(CEMC_ERR_ARG, "trace buffers must be given together");
   if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
   if (r->n_trials == 0) return CEMC_OK;
+  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_SPIN_HALFWARP)
+    return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
+  if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
+  const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
+  if (want_spin && !geo->spin_ok)
+    return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
+  const bool use_spin = want_spin || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
+  const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP;
+  if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
+    return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs single-site flips with at most 16 cluster ECIs");
+  if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && r->cluster == 2)
+    return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs one CTA per chain");
+  // two trials per warp: asked for, or chosen when eligible and no CTA pair was asked for
+  const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
+                                                                r->cluster != 2)) ? 2 : 1;
   int warps = r->warps > 0 ? r->warps : 16;
-  if (warps > cemc::kMaxEval) warps = cemc::kMaxEval;
   const int rsize = r->precision == CEMC_PREC_F32 ? 4 : 8;
   cemc::RunArgs a;
   a.n_chains = r->n_chains;
@@ -373,11 +415,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   a.chain_key = r->chain_key;
   a.accum_slot = r->accum_slot;
   a.chain_trials = r->chain_trials;
-  const bool use_spin = (r->kernel == CEMC_KERNEL_SPIN) || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
-  if (r->kernel == CEMC_KERNEL_SPIN && !geo->spin_ok)
-    return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
+  a.tpw = tpw;
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
-  if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
   // Shared memory: the occupation, then (swaps) the site lists, then exact
   // stamp tables (one entry per site) are preferred; fall back in that order.
   const size_t budget = (size_t)geo->max_smem;
@@ -390,16 +429,18 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   };
   const Choice choices[] = {{1, is_swap, exact_bits}, {1, 0, exact_bits}, {1, 0, 12}, {0, 0, 12}, {0, 0, 5}};
   auto fit = [&](int cl, cemc::McLayout &L, cemc::RunArgs &x) {
-    const int rb = cemc::ring_bits_for(cl);
+    const int w = std::min(warps, cemc::max_eval_warps(cl, tpw));
+    const int rb = cemc::ring_bits_for(cemc::round_trials(cl, w, tpw));
     for (const Choice &ch : choices) {
       for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
-        L = cemc::mc_layout(g, warps, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, use_spin);
+        L = cemc::mc_layout(g, w, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, use_spin, tpw);
         if (L.total <= budget) {
           x.occ_smem = ch.occ;
           x.trk_smem = ch.trk;
           x.stamp_bits = bits;
           x.ring_bits = rb;
           x.cl = cl;
+          x.warps = w;
           return true;
         }
       }
@@ -408,7 +449,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   };
   // Resident cluster pairs of this configuration (cached per geometry).
   auto resident_pairs = [&](const cemc::McLayout &L, const cemc::RunArgs &x) {
-    const auto key = std::make_tuple(warps, (int)r->move, (int)r->precision, (int)use_spin, L.total);
+    const auto key = std::make_tuple(x.warps, (int)r->move, (int)r->precision, (int)use_spin, L.total);
     std::lock_guard<std::mutex> lock(geo->mu);
     auto it = geo->pairs.find(key);
     if (it != geo->pairs.end()) return it->second;
@@ -418,7 +459,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   };
   cemc::McLayout L{};
   bool found = false;
-  if (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms)) {
+  if (tpw == 1 && (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms))) {
     cemc::RunArgs x = a;
     cemc::McLayout L2{};
     if (fit(2, L2, x)) {

@@ -12,6 +12,7 @@ namespace cemc {
 struct RunArgs {
   int n_chains, warps;
   int cl;                  // CTAs per chain (1, or 2 for a thread-block cluster pair)
+  int tpw;                 // trials per evaluating warp and round (2: one per half-warp, spin flips)
   int ring_bits;           // log2 of the draw / neighbour-row ring size
   int occ_smem, trk_smem;  // 1: the chain's occupation / swap tracker lives in shared memory
   int stamp_bits;          // log2 of the size of each of the two conflict-stamp tables
@@ -33,12 +34,22 @@ struct RunArgs {
   uint64_t chunk_offset;  // trials of this chain already run by earlier chunks of the same call
 };
 
-constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two more warps are helpers
-constexpr int kRoundSlots = 64;  // trial records per round: up to 2 CTAs x 30 warps
-constexpr int kPrefetchRounds = 3;  // the helper draws this many rounds of trials ahead
+constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two or three more warps are helpers
+constexpr int kRoundSlots = 64;  // trial records per round (trials per round <= 60)
+constexpr int kPrefetchRounds = 3;  // the fetcher draws this many rounds of trials ahead
 
-// Ring size (log2) for `cl` CTAs per chain: holds kPrefetchRounds rounds of trials.
-__host__ __device__ inline int ring_bits_for(int cl) { return cl == 2 ? 8 : 7; }
+// Trials per round of a launch shape.
+__host__ __device__ inline int round_trials(int cl, int warps, int tpw) { return cl * warps * tpw; }
+// Booker warps per CTA: two when one CTA holds a round of more than 32 trials.
+__host__ __device__ inline int n_bookers(int cl, int warps, int tpw) {
+  return (cl == 1 && round_trials(cl, warps, tpw) > 32) ? 2 : 1;
+}
+// Evaluating warps per CTA that fit next to the helpers in 1024 threads.
+__host__ __device__ inline int max_eval_warps(int cl, int tpw) {
+  return (cl == 1 && tpw == 2) ? 29 : kMaxEval;
+}
+// Ring size (log2): more than kPrefetchRounds rounds of trials.
+__host__ __device__ inline int ring_bits_for(int cw) { return kPrefetchRounds * cw < 128 ? 7 : 8; }
 
 // Per-trial draw, written by the helper warp: site (flips), Philox words.
 struct Draw {
@@ -64,7 +75,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 // Shared-memory carve-up of mc_kernel for `warps` evaluating warps per CTA.
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
                                               int trk_smem, int stamp_bits, int n_cl, int n_masks, int ring_bits,
-                                              bool spin) {
+                                              bool spin, int tpw) {
   McLayout L;
   size_t o = 0;
   const size_t K = (size_t)g.n_eci;
@@ -75,8 +86,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 8 * K);
   L.w = o;
   o = align16(o + 8 * K);
-  L.acc = o;  // per-lane running sums [14][32], then singlets at launch start (4) and 1/N
-  o = align16(o + 8 * (size_t)((2 + 3 * CEMC_MAX_BF) * 32 + CEMC_MAX_BF + 1));
+  L.acc = o;  // per-lane running sums of up to two bookers [2][14][32], then singlets at launch start (4), 1/N
+  o = align16(o + 8 * (size_t)(2 * (2 + 3 * CEMC_MAX_BF) * 32 + CEMC_MAX_BF + 1));
   L.cfw = o;  // per-warp sums of committed correlation-function changes [warps][n_eci]
   o = align16(o + 8 * (size_t)warps * K);
   L.coef = o;
@@ -96,9 +107,9 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   L.sp_masks = o;
   o = align16(o + 8 * (size_t)n_masks);
   L.sp_shift = o;
-  o = align16(o + (size_t)n_masks);
+  o = align16(o + 2 * (size_t)n_masks);  // 32-lane shifts, then 16-lane shifts
   L.sp_lane = o;
-  if (n_cl > 0) o = align16(o + 4 * (33 + 32));
+  if (n_cl > 0) o = align16(o + 4 * (33 + 32 + 17 + 16));
   size_t r = 0;
   L.rec_sa = r;
   r += 4 * S;
@@ -122,7 +133,7 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   L.rec = o;
   o = align16(o + 2 * L.rec_stride);
   L.drow = o;
-  o = align16(o + (size_t)rsize * warps * K);
+  o = align16(o + (size_t)rsize * warps * tpw * K);
   const size_t ring = (size_t)1 << ring_bits;
   L.draws = o;
   o = align16(o + sizeof(Draw) * ring);

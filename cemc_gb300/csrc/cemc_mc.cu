@@ -170,21 +170,24 @@ __device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
   return (double)hi + (double)lo;
 }
 
-template <typename R, int MOVE, bool SPIN, int CL>
+template <typename R, int MOVE, bool SPIN, int CL, int TPW>
 __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
-  const int W = a.warps;  // evaluating warps per CTA; warps W (booker) and W + 1 (fetcher) are helpers
-  const int CW = CL * W;  // trials per round
+  const int W = a.warps;   // evaluating warps per CTA, then NB booker warps and one fetcher warp
+  const int CW = round_trials(CL, W, TPW);  // trials per round
+  const int NB = n_bookers(CL, W, TPW);
   const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits, SPIN ? sd.n_cl : 0,
-                               SPIN ? sd.n_masks : 0, a.ring_bits, SPIN);
+                               SPIN ? sd.n_masks : 0, a.ring_bits, SPIN, TPW);
   const uint32_t rmask = (1u << a.ring_bits) - 1u;
   const int rank = (CL == 2) ? (int)cluster_cta_rank() : 0;
   const unsigned peer = (unsigned)(rank ^ 1);
   const int chain = blockIdx.x / CL;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool helper = (warp >= W);
-  const bool booker = (warp == W), fetcher = (warp == W + 1);
+  const bool booker = helper && warp < W + NB, fetcher = (warp == W + NB);
+  // booker q books trials 32q .. 32q + 31 of each round: q = CTA rank in a pair, else the booker's index
+  const int bq = (CL == 2) ? rank : (booker ? warp - W : 0);
   const int gidx = rank * W + warp;  // this warp's trial slot in a round
   const int N = g.n_sites, n_eci = g.n_eci, cpad = g.cpad;
   const uint32_t hmask = (1u << L.stamp_bits) - 1u;
@@ -202,8 +205,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   using A = typename std::conditional<DF, df64, double>::type;
   constexpr int NACC = 2 + 3 * CEMC_MAX_BF;
   constexpr int NBF = SPIN ? 1 : CEMC_MAX_BF;
-  A *lacc = reinterpret_cast<A *>(smem + L.acc);  // [NACC][32]
-  A *s_start = lacc + NACC * 32;                  // [CEMC_MAX_BF] singlets at launch start, then 1/N
+  A *lacc0 = reinterpret_cast<A *>(smem + L.acc);   // [2][NACC][32], one block per booker of this CTA
+  A *lacc = lacc0 + (CL == 1 ? bq : 0) * NACC * 32;  // this booker's block
+  A *s_start = lacc0 + 2 * NACC * 32;                // [CEMC_MAX_BF] singlets at launch start, then 1/N
   A *cfw = reinterpret_cast<A *>(smem + L.cfw);   // [W][n_eci]
   R *coef_s = reinterpret_cast<R *>(smem + L.coef);
   R *bf_s = reinterpret_cast<R *>(smem + L.bf);
@@ -215,10 +219,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int8_t *dec_s = kind_s + n_eci;
   // misc: [1] status, [2] species present, [4..12) present ids, [12..20) site-list
   //       starts, [20..28) site-list counts, [32..36) round starts written by the peer CTA,
-  //       [36..38) accept count of this CTA's booker
+  //       [36..40) accept counts of this CTA's bookers
   int32_t *misc = reinterpret_cast<int32_t *>(smem + L.misc);
   uint64_t *t0_slot = reinterpret_cast<uint64_t *>(misc + 32);
-  uint64_t *nacc_slot = reinterpret_cast<uint64_t *>(misc + 36);  // the booker's accept count (pairs)
+  uint64_t *nacc_slot = reinterpret_cast<uint64_t *>(misc + 36);  // [2] accept counts of this CTA's bookers
   Draw *draws = reinterpret_cast<Draw *>(smem + L.draws);
   int32_t *rows = reinterpret_cast<int32_t *>(smem + L.rows);
   uint32_t *stamp = reinterpret_cast<uint32_t *>(smem + L.stamp);  // two tables of hmask + 1 entries
@@ -234,6 +238,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   uint8_t *sp_shift = reinterpret_cast<uint8_t *>(smem + L.sp_shift);
   int32_t *sp_lane_term = reinterpret_cast<int32_t *>(smem + L.sp_lane);
   int32_t *sp_lane_first = sp_lane_term + 33;
+  uint8_t *sp_half_shift = sp_shift + (SPIN ? sd.n_masks : 0);
+  int32_t *sp_half_term = sp_lane_first + 32;  // [17]
+  int32_t *sp_half_first = sp_half_term + 17;  // [16]
   const uint32_t xorv = SPIN ? (uint32_t)(sd.minus_id ^ 1) : 0u;  // spin bit = occ ^ xorv (1 = the -1 species)
 
   int8_t *occ = a.occ_smem ? reinterpret_cast<int8_t *>(smem + L.occ) : a.occ + (size_t)chain * N;
@@ -265,19 +272,23 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
   for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
-  for (int i = tid; i < W * n_eci; i += blockDim.x) {
-    cfw[i] = acc_from<A>(0.0);
+  for (int i = tid; i < W * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
+  for (int i = tid; i < TPW * W * n_eci; i += blockDim.x)
     drow[i] = (R)0;  // the spin path writes only the entries of cluster and singlet ECIs
-  }
-  for (int i = tid; i < NACC * 32; i += blockDim.x) lacc[i] = acc_from<A>(0.0);
+  for (int i = tid; i < 2 * NACC * 32; i += blockDim.x) lacc0[i] = acc_from<A>(0.0);
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
     for (int t = tid; t < sd.n_masks; t += blockDim.x) {
       sp_masks[t] = sd.masks[t];
       sp_shift[t] = sd.shift[t];
+      sp_half_shift[t] = TPW == 2 ? sd.half_shift[t] : 0;
     }
     for (int i = tid; i < 33; i += blockDim.x) sp_lane_term[i] = sd.lane_term[i];
     for (int i = tid; i < 32; i += blockDim.x) sp_lane_first[i] = sd.lane_first[i];
+    if (TPW == 2) {
+      for (int i = tid; i < 17; i += blockDim.x) sp_half_term[i] = sd.half_lane_term[i];
+      for (int i = tid; i < 16; i += blockDim.x) sp_half_first[i] = sd.half_lane_first[i];
+    }
   }
   if (a.occ_smem) {
     const int8_t *src = a.occ + (size_t)chain * N;
@@ -293,6 +304,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   if (tid == 0) {
     misc[1] = 0;
     t0_slot[0] = t0_slot[1] = 0;
+    nacc_slot[0] = nacc_slot[1] = 0;
     if (SWAP) {
       int np = 0;
       for (int s = 0; s < g.n_sym; ++s) {
@@ -434,7 +446,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   };
   auto book = [&](const unsigned char *rec, int ks) {
     const int k0 = ks < 32 ? ks : 32, k1 = ks - k0;
-    if (rank == 0) {
+    if (bq == 0) {
       book_half(rec, 0, k0);
       if (k1 > 0) carry_half(rec, 32, k1);
     } else {
@@ -470,14 +482,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   unsigned sp_multi = 0;  // cluster ECIs with multi-site terms
   int sp_tlo = 0, sp_thi = 0, sp_first = 0;  // this lane's range of multi-site terms
   if (SPIN) {
-    sp_tlo = sp_lane_term[lane];
-    sp_thi = sp_lane_term[lane + 1];
-    sp_first = sp_lane_first[lane];
-    if (lane < sd.n_cl) {
-      sp_e = sp_eci[lane];
+    // two trials per warp: lane l works for trial l / 16 on cluster ECI (and term range) l % 16
+    const int el = (TPW == 2) ? (lane & 15) : lane;
+    sp_tlo = TPW == 2 ? sp_half_term[el] : sp_lane_term[el];
+    sp_thi = TPW == 2 ? sp_half_term[el + 1] : sp_lane_term[el + 1];
+    sp_first = TPW == 2 ? sp_half_first[el] : sp_lane_first[el];
+    if (el < sd.n_cl) {
+      sp_e = sp_eci[el];
       sp_coef = coef_s[sp_e.eci];
     }
-    sp_multi = __ballot_sync(kFull, lane < sd.n_cl && sp_e.n_multi > 0);
+    sp_multi = __ballot_sync(kFull, el < sd.n_cl && sp_e.n_multi > 0);
+    if (TPW == 2) sp_multi &= 0xFFFFu;
   }
 
   uint64_t t0 = t_first;
@@ -497,7 +512,92 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     R *r_ds = reinterpret_cast<R *>(rec + L.rec_ds);
     uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
     R *Dw = drow + (size_t)(helper ? 0 : warp) * n_eci;
-    if (!helper) {
+    if (!helper && TPW == 2) {
+      // ---- phase A, two flips per warp: half h = lane / 16 evaluates trial slot 2 warp + h ----
+      if (active && t0 + (uint64_t)(2 * warp) < t_end) {
+        const int h = lane >> 4, hl = lane & 15;
+        const int gh = 2 * warp + h;
+        const uint64_t t = t0 + (uint64_t)gh;
+        const bool has = t < t_end;  // the second half of the last warp may have no trial
+        const uint32_t slot = (uint32_t)t & rmask;
+        int sa = 0, na = 0, oa = 0;
+        uint32_t ua = 0, ub = 0;
+        if (has) {
+          const Draw dr = draws[slot];
+          sa = dr.site;
+          oa = occ[sa];
+          const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
+          na = k + (k >= oa);
+          ua = dr.w2;
+          ub = dr.w3;
+        }
+        const uint32_t occ_a_bit = (uint32_t)oa ^ xorv;
+        // spin word of the neighbour row: bit c = column c, from four ballots of
+        // 16 columns (c = hl + 16 j) of which each half keeps its own 16 bits
+        const int32_t *row = rows + (size_t)slot * cpad;
+        int nbr[4];
+        uint32_t wl = 0, wh = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int c = hl + 16 * j;
+          uint32_t bit = 0;
+          nbr[j] = -1;
+          if (has && c < g.n_cols) {
+            const int sn = row[c];
+            nbr[j] = sn;
+            bit = (uint32_t)occ[sn] ^ xorv;
+          }
+          const uint32_t chunk = (__ballot_sync(kFull, bit) >> (16 * h)) & 0xFFFFu;
+          if (j == 0) wl = chunk;
+          else if (j == 1) wl |= chunk << 16;
+          else if (j == 2) wh = chunk;
+          else wh |= chunk << 16;
+        }
+        const uint32_t pa = spin_lane_parities(sp_masks, sp_half_shift, sp_tlo, sp_thi, wl, wh);
+        // odd-parity counts of each multi-site cluster ECI: one reduction serves
+        // both halves (half h's count in bits 16h .. 16h + 15, at most 16 x 63)
+        int my_odd = 0;
+        for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+          const int k = __ffs(mm) - 1;
+          const int sl = k - sp_first;
+          const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
+          const uint32_t tot = __reduce_add_sync(kFull, v << (16 * h));
+          if (hl == k) my_odd = (int)((tot >> (16 * h)) & 0xFFFFu);
+        }
+        const int delta = occ_a_bit ? 2 : -2;
+        R *Dh = drow + (size_t)gh * n_eci;
+        int P = 0;
+        if (hl < sd.n_cl) {
+          P = sp_e.n_pairs - 2 * (__popc(wl & sp_e.pair_lo) + __popc(wh & sp_e.pair_hi)) + sp_e.n_multi - 2 * my_odd;
+          if (has) Dh[sp_e.eci] = (R)(delta * P);
+        }
+        R sum = sp_coef * (R)P;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        if (sd.singlet_eci >= 0) {
+          if (hl == 0 && has) Dh[sd.singlet_eci] = (R)delta;
+          sum += coef_s[sd.singlet_eci];
+        }
+        const R de = (R)delta * sum;
+        int acc = 0;
+        if (hl == 0 && has) {
+          acc = metropolis<R>(de, ua, ub, kT, inv_kT);
+          r_sa[gh] = sa;
+          r_sb[gh] = na;
+          r_acc[gh] = (int8_t)acc;
+          r_de[gh] = de;
+          r_ds[gh] = (R)delta;  // the singlet change (one decoration)
+        }
+        acc = __shfl_sync(kFull, acc, 16 * h);
+        if (acc) {
+          const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (nbr[j] >= 0) atomicMax(&tab[(uint32_t)nbr[j] & hmask], mark);
+          if (hl == 0) atomicMax(&tab[(uint32_t)sa & hmask], mark);
+        }
+      }
+    } else if (!helper) {
       // ---- phase A: every evaluating warp computes one trial speculatively ----
       const uint64_t t = t0 + (uint64_t)gidx;
       if (active && t < t_end) {
@@ -689,19 +789,25 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         }
       }
       __syncwarp();
-      if (gidx < ks) {
-        if (r_acc[gidx]) {
-          // this warp's committed accepted trial: add its change row to the warp's sums
-          A *cw = cfw + (size_t)warp * n_eci;
-          for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], Dw[k]);
+#pragma unroll
+      for (int h2 = 0; h2 < TPW; ++h2) {
+        const int go = (TPW == 2) ? 2 * warp + h2 : gidx;  // this warp's trial slot(s)
+        if (go < ks) {
+          if (r_acc[go]) {
+            // this warp's committed accepted trial: add its change row to the warp's sums
+            const R *D = drow + (size_t)(TPW * warp + h2) * n_eci;
+            A *cw = cfw + (size_t)warp * n_eci;
+            for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], D[k]);
+          }
+          if (a.trace_acc && lane == 0) {
+            const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + go - t_first);
+            a.trace_site[2 * idx] = r_sa[go];
+            a.trace_site[2 * idx + 1] = r_sb[go];
+            a.trace_acc[idx] = r_acc[go];
+            a.trace_de[idx] = (double)r_de[go];
+          }
         }
-        if (a.trace_acc && lane == 0) {
-          const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + gidx - t_first);
-          a.trace_site[2 * idx] = r_sa[gidx];
-          a.trace_site[2 * idx + 1] = r_sb[gidx];
-          a.trace_acc[idx] = r_acc[gidx];
-          a.trace_de[idx] = (double)r_de[gidx];
-        }
+        __syncwarp();
       }
     }
     ks_prev = ks;
@@ -710,8 +816,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
 
   if (fetcher) cp_async_wait_all();
+  if (CL == 1 && booker && lane == 0) nacc_slot[bq] = n_acc_launch;
   if (CL == 2) {
-    if (booker && lane == 0) nacc_slot[0] = n_acc_launch;
+    if (booker && lane == 0) nacc_slot[CL == 1 ? bq : 0] = n_acc_launch;
     cluster_barrier();  // the peer's sums are final and readable
   } else {
     __syncthreads();
@@ -720,7 +827,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   // ---- epilogue --------------------------------------------------------------
   const bool ok = misc[1] == 0;
   double sum_v = 0.0;         // thread tid < NACC: running sum `tid` over the bookers' lanes
-  uint64_t n_acc_total = 0;   // CTA 0's booker: accepted trials of the launch
+  uint64_t n_acc_total = 0;   // thread 0 of CTA 0: accepted trials of the launch
   if (rank == 0 && ok) {
     // the launch's correlation-function changes: per-warp sums of both CTAs in
     // warp order (exact for integer-valued changes), then one scaling per ECI
@@ -734,12 +841,13 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
     }
     if (a.accum && tid < NACC) {
-      for (int l = 0; l < 32; ++l) sum_v += acc_to(lacc[tid * 32 + l]);
+      for (int q = 0; q < NB; ++q)
+        for (int l = 0; l < 32; ++l) sum_v += acc_to(lacc0[(q * NACC + tid) * 32 + l]);
       if (CL == 2)
-        for (int l = 0; l < 32; ++l) sum_v += ld_peer_acc(&lacc[tid * 32 + l], peer);
+        for (int l = 0; l < 32; ++l) sum_v += ld_peer_acc(&lacc0[tid * 32 + l], peer);
     }
-    if (booker && lane == 0) {
-      n_acc_total = n_acc_launch;
+    if (tid == 0) {
+      n_acc_total = nacc_slot[0] + nacc_slot[1];
       if (CL == 2) {
         uint64_t v;
         asm volatile("ld.shared::cluster.u64 %0, [%1];\n" : "=l"(v) : "r"(peer_addr(nacc_slot, peer)) : "memory");
@@ -773,7 +881,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       sums[tid] += sum_v;
     }
   }
-  if (booker && lane == 0) {
+  if (tid == 0) {
     // energy = N * eci . cf in sorted-name order (ce_updater.cpp:236-242)
     double e = 0.0;
     for (int k = 0; k < n_eci; ++k) e += eci_s[k] * cf_s[k];
@@ -788,14 +896,19 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
 }
 
-template <typename R, int MOVE, bool SPIN, int CL>
+// Threads of one CTA: evaluating warps, bookers, fetcher.
+static unsigned block_threads(const RunArgs &a) {
+  return (unsigned)((a.warps + n_bookers(a.cl, a.warps, a.tpw) + 1) * 32);
+}
+
+template <typename R, int MOVE, bool SPIN, int CL, int TPW>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
-  auto k = mc_kernel<R, MOVE, SPIN, CL>;
+  auto k = mc_kernel<R, MOVE, SPIN, CL, TPW>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_chains * CL));
-  cfg.blockDim = dim3((unsigned)((a.warps + 2) * 32));
+  cfg.blockDim = dim3(block_threads(a));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -810,17 +923,17 @@ static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cuda
   return cudaGetLastError();
 }
 
-template <typename R, int MOVE, bool SPIN, int CL>
+template <typename R, int MOVE, bool SPIN>
 static int clusters_t(const RunArgs &a, size_t smem) {
-  auto k = mc_kernel<R, MOVE, SPIN, CL>;
+  auto k = mc_kernel<R, MOVE, SPIN, 2, 1>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(a.n_chains * CL));
-  cfg.blockDim = dim3((unsigned)((a.warps + 2) * 32));
+  cfg.gridDim = dim3((unsigned)(a.n_chains * 2));
+  cfg.blockDim = dim3(block_threads(a));
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.x = 2;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -833,34 +946,41 @@ static int clusters_t(const RunArgs &a, size_t smem) {
   return n;
 }
 
-template <bool SPIN, int CL>
-static cudaError_t launch_p(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
-                            const SpinDev &sd) {
-  if (precision == CEMC_PREC_F32)
-    return move == CEMC_MOVE_SWAP ? launch_t<float, CEMC_MOVE_SWAP, SPIN, CL>(g, a, smem, st, sd)
-                                  : launch_t<float, CEMC_MOVE_FLIP, SPIN, CL>(g, a, smem, st, sd);
-  return move == CEMC_MOVE_SWAP ? launch_t<double, CEMC_MOVE_SWAP, SPIN, CL>(g, a, smem, st, sd)
-                                : launch_t<double, CEMC_MOVE_FLIP, SPIN, CL>(g, a, smem, st, sd);
+template <typename R>
+static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t smem, cudaStream_t st,
+                            const SpinDev *spin) {
+  const SpinDev none{};
+  if (move == CEMC_MOVE_SWAP) {
+    if (spin) return a.cl == 2 ? launch_t<R, CEMC_MOVE_SWAP, true, 2, 1>(g, a, smem, st, *spin)
+                               : launch_t<R, CEMC_MOVE_SWAP, true, 1, 1>(g, a, smem, st, *spin);
+    return a.cl == 2 ? launch_t<R, CEMC_MOVE_SWAP, false, 2, 1>(g, a, smem, st, none)
+                     : launch_t<R, CEMC_MOVE_SWAP, false, 1, 1>(g, a, smem, st, none);
+  }
+  if (spin) {
+    if (a.tpw == 2) return launch_t<R, CEMC_MOVE_FLIP, true, 1, 2>(g, a, smem, st, *spin);
+    return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, true, 2, 1>(g, a, smem, st, *spin)
+                     : launch_t<R, CEMC_MOVE_FLIP, true, 1, 1>(g, a, smem, st, *spin);
+  }
+  return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, false, 2, 1>(g, a, smem, st, none)
+                   : launch_t<R, CEMC_MOVE_FLIP, false, 1, 1>(g, a, smem, st, none);
 }
 
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       const SpinDev *spin) {
-  if (a.cl == 2) {
-    if (spin) return launch_p<true, 2>(g, a, move, precision, smem, st, *spin);
-    return launch_p<false, 2>(g, a, move, precision, smem, st, SpinDev{});
-  }
-  if (spin) return launch_p<true, 1>(g, a, move, precision, smem, st, *spin);
-  return launch_p<false, 1>(g, a, move, precision, smem, st, SpinDev{});
+  // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
+  if (a.tpw == 2 && (!spin || move != CEMC_MOVE_FLIP || a.cl != 1)) return cudaErrorInvalidValue;
+  return precision == CEMC_PREC_F32 ? launch_r<float>(g, a, move, smem, st, spin)
+                                    : launch_r<double>(g, a, move, smem, st, spin);
 }
 
 int max_active_clusters(const DevGeo &, const RunArgs &a, int move, int precision, size_t smem, bool spin) {
   const bool f32 = precision == CEMC_PREC_F32, swap = move == CEMC_MOVE_SWAP;
   if (spin) {
-    if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, true, 2>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, true, 2>(a, smem);
-    return swap ? clusters_t<double, CEMC_MOVE_SWAP, true, 2>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, true, 2>(a, smem);
+    if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, true>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, true>(a, smem);
+    return swap ? clusters_t<double, CEMC_MOVE_SWAP, true>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, true>(a, smem);
   }
-  if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, false, 2>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, false, 2>(a, smem);
-  return swap ? clusters_t<double, CEMC_MOVE_SWAP, false, 2>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, false, 2>(a, smem);
+  if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, false>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, false>(a, smem);
+  return swap ? clusters_t<double, CEMC_MOVE_SWAP, false>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, false>(a, smem);
 }
 
 }  // namespace cemc

@@ -33,6 +33,12 @@ struct SpinDev {
   const uint8_t *shift;      // [n_masks]
   const int32_t *lane_term;  // [33]
   const int32_t *lane_first; // [32]
+  // Half-warp form (one flip per 16 lanes): the same terms cut into 16 lane
+  // ranges; usable when half_ok (at most 16 cluster ECIs, counters fit).
+  int half_ok;
+  const uint8_t *half_shift;       // [n_masks]
+  const int32_t *half_lane_term;   // [17]
+  const int32_t *half_lane_first;  // [16]
 };
 
 }  // namespace cemc

@@ -25,6 +25,7 @@ PREC_F32 = _lib.PREC_F32
 KERNEL_AUTO = _lib.KERNEL_AUTO
 KERNEL_GENERIC = _lib.KERNEL_GENERIC
 KERNEL_SPIN = _lib.KERNEL_SPIN
+KERNEL_SPIN_HALFWARP = _lib.KERNEL_SPIN_HALFWARP
 ACCUM_DOUBLES = _lib.ACCUM_DOUBLES
 # Field offsets (in doubles) of cemc_accum.
 A_EREF, A_SUM_E, A_SUM_E2, A_SUM_S, A_SUM_S2, A_SUM_SE, A_NSAMP, A_NACC = 0, 1, 2, 3, 7, 11, 15, 16

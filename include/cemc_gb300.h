@@ -138,14 +138,19 @@ typedef struct {
                           per round), or 0 = 2 when every chain's pair fits on the GPU at once, else 1 */
 } cemc_run_desc;
 
-/* Kernel selection of cemc_run.  AUTO takes the binary spin-basis kernel when
+/* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when
  * the geometry allows it (two species with basis values +1 and -1, at most 64
- * neighbour columns, at most 32 cluster ECIs), else the generic one.  Both give
- * the same decisions for the same stream; the spin kernel evaluates one trial
- * per lane with bit-packed neighbourhoods. */
+ * neighbour columns, at most 32 cluster ECIs), else the generic one; for
+ * single-site flips with at most 16 cluster ECIs and no CTA pair asked for it
+ * takes the half-warp spin form.  All give the same decisions for the same
+ * stream.  The spin forms evaluate a trial from a bit-packed neighbourhood
+ * (popcounts of shell masks, parities of multi-site terms), one trial per warp
+ * or, half-warp form, one per 16 lanes; the generic form multiplies basis
+ * values term by term. */
 #define CEMC_KERNEL_AUTO 0
 #define CEMC_KERNEL_GENERIC 1
 #define CEMC_KERNEL_SPIN 2
+#define CEMC_KERNEL_SPIN_HALFWARP 3  /* spin basis, flips only, two trials per warp (one per 16 lanes) */
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
  * energy change, accept test and in-place commit of occupation, correlation

@@ -52,13 +52,16 @@ def _run_shape(cb, n, E, **kw):
         raise
 
 
-def _kernel_ok(m, kernel, E):
-    """The spin-basis kernel only takes binary +1/-1 geometries."""
-    if kernel == E.KERNEL_SPIN and not (m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0]):
+def _kernel_ok(m, kernel, E, move=0, cluster=0):
+    """The spin-basis kernels only take binary +1/-1 geometries; the half-warp one only flips on one CTA."""
+    if kernel in (E.KERNEL_SPIN, E.KERNEL_SPIN_HALFWARP) and not (
+            m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0]):
         pytest.skip("spin-basis kernel needs a binary +1/-1 basis")
+    if kernel == E.KERNEL_SPIN_HALFWARP and (move != 0 or cluster == 2):
+        pytest.skip("the half-warp spin kernel runs flips on one CTA per chain")
 
 
-KERNELS = [1, 2]  # generic, spin
+KERNELS = [1, 2, 3]  # generic, spin, spin half-warp
 CLUSTERS = [1, 2]  # CTAs per chain
 
 
@@ -69,7 +72,7 @@ CLUSTERS = [1, 2]  # CTAs per chain
 def test_gpu_replays_reference_fixture_fp64(case, warps, kernel, cluster, E):
     g = load_golden(case)
     s, m, eci = golden_model(g)
-    _kernel_ok(m, kernel, E)
+    _kernel_ok(m, kernel, E, int(g["move"]), cluster)
     geo = E.Geometry(m)
     move = int(g["move"])
     cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=int(g["seed"]))
@@ -93,7 +96,7 @@ def test_gpu_replays_reference_fixture_fp64(case, warps, kernel, cluster, E):
 def test_gpu_fp32_energy_change_against_reference_fixture(case, kernel, cluster, E):
     g = load_golden(case)
     s, m, eci = golden_model(g)
-    _kernel_ok(m, kernel, E)
+    _kernel_ok(m, kernel, E, int(g["move"]), cluster)
     geo = E.Geometry(m)
     cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), int(g["move"]), seed=int(g["seed"]))
     n = int(g["n_trials"])
@@ -180,6 +183,7 @@ def test_gpu_batch_equals_oracle_per_chain(move, prec, kernel, cluster, E, oracl
     """Many chains in one launch, each equal to the oracle run of that chain (keys, temperatures, mu differ)."""
     g = load_golden("binary_flip")
     s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E, move, cluster)
     geo = E.Geometry(m)
     orc = oracle_mod.Oracle(m)
     rng = np.random.default_rng(7)
@@ -213,15 +217,21 @@ def test_gpu_batch_equals_oracle_per_chain(move, prec, kernel, cluster, E, oracl
 
 @pytest.mark.parametrize("kernel", KERNELS)
 def test_gpu_launch_splitting_is_invisible(kernel, E):
-    """k launches of n/k trials equal one launch of n (counter-based proposals, resident state)."""
-    g = load_golden("binary_swap")
+    """k launches of n/k trials equal one launch of n (counter-based proposals, resident state),
+    whatever the launch shape of each piece (warps, CTAs per chain, trials per warp)."""
+    half = kernel == E.KERNEL_SPIN_HALFWARP
+    g = load_golden("binary_flip" if half else "binary_swap")
+    move = 0 if half else 1
     s, m, eci = golden_model(g)
     geo = E.Geometry(m)
-    a = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
-    b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=4)
+    a = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=4)
+    b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=4)
     a.run(3000, precision=0, warps=16, kernel=kernel, cluster=1)
     for i in range(3):
-        b.run(1000, precision=0, warps=7, kernel=kernel, cluster=2 - i % 2)
+        if i == 1:  # the middle piece on a CTA pair (the half-warp form runs one CTA: use the warp-per-trial form)
+            b.run(1000, precision=0, warps=7, kernel=E.KERNEL_SPIN if half else kernel, cluster=2)
+        else:
+            b.run(1000, precision=0, warps=7, kernel=kernel, cluster=1)
     _sync()
     assert np.array_equal(a.occ.cpu().numpy(), b.occ.cpu().numpy())
     assert np.allclose(a.cf.cpu().numpy(), b.cf.cpu().numpy(), rtol=1e-12, atol=1e-15)
@@ -236,6 +246,7 @@ def test_gpu_launch_splitting_is_invisible(kernel, E):
 def test_gpu_accumulators_match_oracle(kernel, cluster, E, oracle_mod):
     g = load_golden("binary_flip")
     s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E, 0, cluster)
     geo = E.Geometry(m)
     orc = oracle_mod.Oracle(m)
     for prec in (0, 1):
