@@ -62,7 +62,7 @@ struct McLayout {
   size_t sp_eci, sp_masks, sp_shift, sp_lane;  // spin-basis tables (empty unless n_cl > 0)
   // per-round trial records (two buffers, by round parity), kRoundSlots entries each
   size_t rec, rec_stride, rec_sa, rec_sb, rec_de, rec_ds, rec_acc, rec_la, rec_lb, rec_A, rec_B;
-  size_t drow;  // [warps][n_eci] correlation-function changes of each warp's own trial
+  size_t drow;  // [2][warps * tpw][n_eci] correlation-function changes of this CTA's trials
   size_t draws, rows;
   size_t warp0, warp_stride, warp_part;
   size_t occ, trk, stamp;
@@ -88,8 +88,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 8 * K);
   L.acc = o;  // per-lane running sums of up to two bookers [2][14][32], then singlets at launch start (4), 1/N
   o = align16(o + 8 * (size_t)(2 * (2 + 3 * CEMC_MAX_BF) * 32 + CEMC_MAX_BF + 1));
-  L.cfw = o;  // per-warp sums of committed correlation-function changes [warps][n_eci]
-  o = align16(o + 8 * (size_t)warps * K);
+  L.cfw = o;  // per-booker sums of committed correlation-function changes [2][n_eci]
+  o = align16(o + 8 * 2 * K);
   L.coef = o;
   o = align16(o + (size_t)rsize * K);
   L.bf = o;
@@ -104,10 +104,9 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 4 * 64);
   L.sp_eci = o;
   o = align16(o + 32 * (size_t)n_cl);
-  L.sp_masks = o;
-  o = align16(o + 8 * (size_t)n_masks);
-  L.sp_shift = o;
-  o = align16(o + 2 * (size_t)n_masks);  // 32-lane shifts, then 16-lane shifts
+  L.sp_masks = o;  // per multi-site term: {mask lo, mask hi, 32-lane shift, 16-lane shift}
+  o = align16(o + 16 * (size_t)n_masks);
+  L.sp_shift = o;  // (unused)
   L.sp_lane = o;
   if (n_cl > 0) o = align16(o + 4 * (33 + 32 + 17 + 16));
   size_t r = 0;
@@ -132,8 +131,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   L.rec_stride = align16(r);
   L.rec = o;
   o = align16(o + 2 * L.rec_stride);
-  L.drow = o;
-  o = align16(o + (size_t)rsize * warps * tpw * K);
+  L.drow = o;  // two buffers (round parity) of [warps * tpw][n_eci]
+  o = align16(o + 2 * (size_t)rsize * warps * tpw * K);
   const size_t ring = (size_t)1 << ring_bits;
   L.draws = o;
   o = align16(o + sizeof(Draw) * ring);

@@ -39,15 +39,17 @@
 // start before each barrier; a mismatch stops both with CEMC_ERR_INTERNAL
 // instead of letting them wait at different barriers.
 //
-// Two extra helper warps per CTA run off the critical path.  The fetcher
+// Two or three helper warps per CTA run off the critical path.  The fetcher
 // precomputes the counter-based draws (philox.h) of upcoming trials and
 // prefetches their neighbour-table rows from L2/HBM into a shared-memory ring
 // with cp.async (single-site flips, whose site does not depend on the state).
-// The booker folds the previous round's records into per-lane running sums of
-// energy and singlets (in a pair, CTA q takes trials 32q .. 32q + 31 of each
-// round and carries the other half's totals).  Each evaluating warp adds the correlation-function changes of its
-// own committed accepted trials to per-warp sums; correlation functions and
-// energy are brought up to date in FP64 once, at the end of the launch.
+// One or two bookers fold each finished round, one round late: booker q keeps
+// per-lane running sums of energy and singlets for trials 32q .. 32q + 31 of
+// each round (carrying the other half's totals), writes their trace entries,
+// and adds the correlation-function changes of its CTA's committed accepted
+// trials (change rows double-buffered by round parity) to a row of sums.
+// Correlation functions and energy are brought up to date in FP64 once, at
+// the end of the launch.
 #include <cuda_runtime.h>
 
 #include <type_traits>
@@ -110,12 +112,15 @@ __device__ __forceinline__ void spin_ballot(const DevGeo &g, const int8_t *occ, 
 }
 
 // Parities of this lane's multi-site terms, packed 6 bits per cluster-ECI slot.
-__device__ __forceinline__ uint32_t spin_lane_parities(const uint2 *masks, const uint8_t *shift, int lo_t, int hi_t,
-                                                       uint32_t lo, uint32_t hi) {
+// terms[t] = {mask lo, mask hi, shift in the 32-lane cut, shift in the 16-lane cut}.
+template <bool HALF>
+__device__ __forceinline__ uint32_t spin_lane_parities(const uint4 *terms, int lo_t, int hi_t, uint32_t lo,
+                                                       uint32_t hi) {
   uint32_t packed = 0;
+#pragma unroll 4
   for (int t = lo_t; t < hi_t; ++t) {
-    const uint2 m = masks[t];
-    packed += (uint32_t)(__popc((lo & m.x) ^ (hi & m.y)) & 1) << shift[t];
+    const uint4 m = terms[t];
+    packed += (uint32_t)(__popc((lo & m.x) ^ (hi & m.y)) & 1) << (HALF ? m.w : m.z);
   }
   return packed;
 }
@@ -197,8 +202,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   double *w_s = reinterpret_cast<double *>(smem + L.w);
   // Running sums of this launch, FP64 in FP64 mode and double-float in FP32
   // mode.  The thermodynamic sums are kept per lane of the booker warps
-  // (lane j of CTA q takes trial 32q + j of each round) and the committed
-  // correlation-function changes per evaluating warp, so no round needs a
+  // (lane j of booker q takes trial 32q + j of each round) and the committed
+  // correlation-function changes per booker and ECI, so no round needs a
   // cross-lane or cross-warp reduction of them; both are reduced once, in
   // fixed order, in the epilogue.
   constexpr bool DF = (sizeof(R) == 4);
@@ -208,7 +213,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   A *lacc0 = reinterpret_cast<A *>(smem + L.acc);   // [2][NACC][32], one block per booker of this CTA
   A *lacc = lacc0 + (CL == 1 ? bq : 0) * NACC * 32;  // this booker's block
   A *s_start = lacc0 + 2 * NACC * 32;                // [CEMC_MAX_BF] singlets at launch start, then 1/N
-  A *cfw = reinterpret_cast<A *>(smem + L.cfw);   // [W][n_eci]
+  A *cfw = reinterpret_cast<A *>(smem + L.cfw);   // [2][n_eci], one row per booker of this CTA
   R *coef_s = reinterpret_cast<R *>(smem + L.coef);
   R *bf_s = reinterpret_cast<R *>(smem + L.bf);
   uint16_t *terms_s = reinterpret_cast<uint16_t *>(smem + L.terms);
@@ -227,18 +232,18 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int32_t *rows = reinterpret_cast<int32_t *>(smem + L.rows);
   uint32_t *stamp = reinterpret_cast<uint32_t *>(smem + L.stamp);  // two tables of hmask + 1 entries
   unsigned char *rec0 = smem + L.rec;
-  R *drow = reinterpret_cast<R *>(smem + L.drow);
+  // change rows of this CTA's trials: exact integers in the spin basis
+  using DT = typename std::conditional<SPIN, int32_t, R>::type;
+  DT *drow = reinterpret_cast<DT *>(smem + L.drow);
   unsigned char *wbase = smem + L.warp0 + (size_t)(helper ? 0 : warp) * L.warp_stride;
   R *va = reinterpret_cast<R *>(wbase);
   R *vb = va + g.vals_len;
   R *part = reinterpret_cast<R *>(wbase + L.warp_part);
 
   SpinEci *sp_eci = reinterpret_cast<SpinEci *>(smem + L.sp_eci);
-  uint2 *sp_masks = reinterpret_cast<uint2 *>(smem + L.sp_masks);
-  uint8_t *sp_shift = reinterpret_cast<uint8_t *>(smem + L.sp_shift);
+  uint4 *sp_terms = reinterpret_cast<uint4 *>(smem + L.sp_masks);
   int32_t *sp_lane_term = reinterpret_cast<int32_t *>(smem + L.sp_lane);
   int32_t *sp_lane_first = sp_lane_term + 33;
-  uint8_t *sp_half_shift = sp_shift + (SPIN ? sd.n_masks : 0);
   int32_t *sp_half_term = sp_lane_first + 32;  // [17]
   int32_t *sp_half_first = sp_half_term + 17;  // [16]
   const uint32_t xorv = SPIN ? (uint32_t)(sd.minus_id ^ 1) : 0u;  // spin bit = occ ^ xorv (1 = the -1 species)
@@ -272,17 +277,14 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
   for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
-  for (int i = tid; i < W * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
-  for (int i = tid; i < TPW * W * n_eci; i += blockDim.x)
-    drow[i] = (R)0;  // the spin path writes only the entries of cluster and singlet ECIs
+  for (int i = tid; i < 2 * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
+  for (int i = tid; i < 2 * TPW * W * n_eci; i += blockDim.x)
+    drow[i] = (DT)0;  // the spin path writes only the entries of cluster and singlet ECIs
   for (int i = tid; i < 2 * NACC * 32; i += blockDim.x) lacc0[i] = acc_from<A>(0.0);
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
-    for (int t = tid; t < sd.n_masks; t += blockDim.x) {
-      sp_masks[t] = sd.masks[t];
-      sp_shift[t] = sd.shift[t];
-      sp_half_shift[t] = TPW == 2 ? sd.half_shift[t] : 0;
-    }
+    for (int t = tid; t < sd.n_masks; t += blockDim.x)
+      sp_terms[t] = make_uint4(sd.masks[t].x, sd.masks[t].y, sd.shift[t], TPW == 2 ? sd.half_shift[t] : 0u);
     for (int i = tid; i < 33; i += blockDim.x) sp_lane_term[i] = sd.lane_term[i];
     for (int i = tid; i < 32; i += blockDim.x) sp_lane_first[i] = sd.lane_first[i];
     if (TPW == 2) {
@@ -380,13 +382,22 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   // Lane j takes trial off + j: one inclusive scan gives the energy and singlet
   // offsets after each trial, and each lane adds its own values to its own
   // sums; a half without accepted trials needs no scan.
-  auto book_half = [&](const unsigned char *rec, int off, int kh) {
+  auto book_half = [&](const unsigned char *rec, int off, int kh, uint64_t tb) {
     const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
     const R *r_de = reinterpret_cast<const R *>(rec + L.rec_de);
     const R *r_ds = reinterpret_cast<const R *>(rec + L.rec_ds);
     const int gg = off + lane;
     const bool mine = lane < kh;
     const bool acc = mine && r_acc[gg];
+    if (a.trace_acc && mine) {  // the round started at trial tb
+      const int32_t *r_sa = reinterpret_cast<const int32_t *>(rec + L.rec_sa);
+      const int32_t *r_sb = reinterpret_cast<const int32_t *>(rec + L.rec_sb);
+      const size_t idx = (size_t)chain * a.n_trials + (size_t)(tb + (uint64_t)gg - t_first);
+      a.trace_site[2 * idx] = r_sa[gg];
+      a.trace_site[2 * idx + 1] = r_sb[gg];
+      a.trace_acc[idx] = r_acc[gg];
+      a.trace_de[idx] = (double)r_de[gg];
+    }
     const unsigned am = __ballot_sync(kFull, acc);
     n_acc_launch += (uint64_t)__popc(am);
     if (!a.accum) return;
@@ -444,15 +455,51 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     for (int b = 0; b < NBF; ++b)
       if (b < g.n_bf) dsum[b] = acc_add_x(dsum[b], warp_sum(acc ? r_ds[b * kRoundSlots + gg] : (R)0));
   };
-  auto book = [&](const unsigned char *rec, int ks) {
+  // Correlation-function changes of this CTA's committed accepted trials in
+  // slots [own_lo, own_hi) (change rows dbuf[slot - own_lo] in a pair, dbuf[slot]
+  // otherwise), summed by the booker: lane takes ECIs lane, lane + 32, ... in
+  // registers; exact 64-bit integers for the spin basis (integer changes).
+  const int own_lo = (CL == 2) ? rank * W : 32 * bq;
+  const int own_hi = (CL == 2) ? own_lo + W : own_lo + 32;
+  A *cfb = cfw + (size_t)(CL == 1 ? bq : 0) * n_eci;
+  using CFA = typename std::conditional<SPIN, long long, A>::type;
+  CFA cfr[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) cfr[i] = CFA{};
+  auto cf_add = [](CFA &c, DT d) {
+    if constexpr (SPIN) c += (long long)d;
+    else c = acc_add_x(c, d);
+  };
+  auto cf_sum_out = [](const CFA &c) -> A {
+    if constexpr (SPIN) return acc_from<A>((double)c);
+    else return c;
+  };
+  auto book_cf = [&](const unsigned char *rec, const DT *dbuf, int ks) {
+    const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
+    const int hi = ks < own_hi ? ks : own_hi;
+    const int j = own_lo + lane;
+    unsigned am = __ballot_sync(kFull, j < hi && r_acc[j]);
+    while (am) {
+      const int jj = own_lo + __ffs(am) - 1;
+      am &= am - 1;
+      const DT *D = dbuf + (size_t)(jj - (CL == 2 ? own_lo : 0)) * n_eci;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k = lane + 32 * i;
+        if (k < n_eci) cf_add(cfr[i], D[k]);
+      }
+    }
+  };
+  auto book = [&](const unsigned char *rec, const DT *dbuf, int ks, uint64_t tb) {
     const int k0 = ks < 32 ? ks : 32, k1 = ks - k0;
     if (bq == 0) {
-      book_half(rec, 0, k0);
+      book_half(rec, 0, k0, tb);
       if (k1 > 0) carry_half(rec, 32, k1);
     } else {
       carry_half(rec, 0, k0);
-      if (k1 > 0) book_half(rec, 32, k1);
+      if (k1 > 0) book_half(rec, 32, k1, tb);
     }
+    book_cf(rec, dbuf, ks);
   };
 
   // Store into this CTA's shared memory and, in a pair, the peer's copy.
@@ -495,267 +542,26 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     if (TPW == 2) sp_multi &= 0xFFFFu;
   }
 
-  uint64_t t0 = t_first;
-  uint32_t round = 1;
-  int ks_prev = 0;
-  while (true) {
-    const bool active = t0 < t_end;
-    unsigned char *rec = rec0 + (size_t)(round & 1) * L.rec_stride;
-    int32_t *r_sa = reinterpret_cast<int32_t *>(rec + L.rec_sa);
-    int32_t *r_sb = reinterpret_cast<int32_t *>(rec + L.rec_sb);
-    int32_t *r_la = reinterpret_cast<int32_t *>(rec + L.rec_la);
-    int32_t *r_lb = reinterpret_cast<int32_t *>(rec + L.rec_lb);
-    int8_t *r_acc = reinterpret_cast<int8_t *>(rec + L.rec_acc);
-    int8_t *r_A = reinterpret_cast<int8_t *>(rec + L.rec_A);
-    int8_t *r_B = reinterpret_cast<int8_t *>(rec + L.rec_B);
-    R *r_de = reinterpret_cast<R *>(rec + L.rec_de);
-    R *r_ds = reinterpret_cast<R *>(rec + L.rec_ds);
-    uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
-    R *Dw = drow + (size_t)(helper ? 0 : warp) * n_eci;
-    if (!helper && TPW == 2) {
-      // ---- phase A, two flips per warp: half h = lane / 16 evaluates trial slot 2 warp + h ----
-      if (active && t0 + (uint64_t)(2 * warp) < t_end) {
-        const int h = lane >> 4, hl = lane & 15;
-        const int gh = 2 * warp + h;
-        const uint64_t t = t0 + (uint64_t)gh;
-        const bool has = t < t_end;  // the second half of the last warp may have no trial
-        const uint32_t slot = (uint32_t)t & rmask;
-        int sa = 0, na = 0, oa = 0;
-        uint32_t ua = 0, ub = 0;
-        if (has) {
-          const Draw dr = draws[slot];
-          sa = dr.site;
-          oa = occ[sa];
-          const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
-          na = k + (k >= oa);
-          ua = dr.w2;
-          ub = dr.w3;
-        }
-        const uint32_t occ_a_bit = (uint32_t)oa ^ xorv;
-        // spin word of the neighbour row: bit c = column c, from four ballots of
-        // 16 columns (c = hl + 16 j) of which each half keeps its own 16 bits
-        const int32_t *row = rows + (size_t)slot * cpad;
-        int nbr[4];
-        uint32_t wl = 0, wh = 0;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int c = hl + 16 * j;
-          uint32_t bit = 0;
-          nbr[j] = -1;
-          if (has && c < g.n_cols) {
-            const int sn = row[c];
-            nbr[j] = sn;
-            bit = (uint32_t)occ[sn] ^ xorv;
-          }
-          const uint32_t chunk = (__ballot_sync(kFull, bit) >> (16 * h)) & 0xFFFFu;
-          if (j == 0) wl = chunk;
-          else if (j == 1) wl |= chunk << 16;
-          else if (j == 2) wh = chunk;
-          else wh |= chunk << 16;
-        }
-        const uint32_t pa = spin_lane_parities(sp_masks, sp_half_shift, sp_tlo, sp_thi, wl, wh);
-        // odd-parity counts of each multi-site cluster ECI: one reduction serves
-        // both halves (half h's count in bits 16h .. 16h + 15, at most 16 x 63)
-        int my_odd = 0;
-        for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
-          const int k = __ffs(mm) - 1;
-          const int sl = k - sp_first;
-          const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
-          const uint32_t tot = __reduce_add_sync(kFull, v << (16 * h));
-          if (hl == k) my_odd = (int)((tot >> (16 * h)) & 0xFFFFu);
-        }
-        const int delta = occ_a_bit ? 2 : -2;
-        R *Dh = drow + (size_t)gh * n_eci;
-        int P = 0;
-        if (hl < sd.n_cl) {
-          P = sp_e.n_pairs - 2 * (__popc(wl & sp_e.pair_lo) + __popc(wh & sp_e.pair_hi)) + sp_e.n_multi - 2 * my_odd;
-          if (has) Dh[sp_e.eci] = (R)(delta * P);
-        }
-        R sum = sp_coef * (R)P;
-#pragma unroll
-        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-        if (sd.singlet_eci >= 0) {
-          if (hl == 0 && has) Dh[sd.singlet_eci] = (R)delta;
-          sum += coef_s[sd.singlet_eci];
-        }
-        const R de = (R)delta * sum;
-        int acc = 0;
-        if (hl == 0 && has) {
-          acc = metropolis<R>(de, ua, ub, kT, inv_kT);
-          r_sa[gh] = sa;
-          r_sb[gh] = na;
-          r_acc[gh] = (int8_t)acc;
-          r_de[gh] = de;
-          r_ds[gh] = (R)delta;  // the singlet change (one decoration)
-        }
-        acc = __shfl_sync(kFull, acc, 16 * h);
-        if (acc) {
-          const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (nbr[j] >= 0) atomicMax(&tab[(uint32_t)nbr[j] & hmask], mark);
-          if (hl == 0) atomicMax(&tab[(uint32_t)sa & hmask], mark);
-        }
-      }
-    } else if (!helper) {
-      // ---- phase A: every evaluating warp computes one trial speculatively ----
-      const uint64_t t = t0 + (uint64_t)gidx;
-      if (active && t < t_end) {
-        const uint32_t slot = (uint32_t)t & rmask;
-        const Draw dr = draws[slot];
-        int sa, sb = -1, na, A_ = 0, B_ = 0;
-        int nbra[4], nbrb[4] = {-1, -1, -1, -1};
-        uint32_t ua, ub;
-        uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
-        if (!SWAP) {
-          sa = dr.site;
-          const int oa = occ[sa];
-          const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
-          na = k + (k >= oa);
-          ua = dr.w2;
-          ub = dr.w3;
-          if (!SPIN) {
-            gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
-          } else {
-            occ_a_bit = (uint32_t)oa ^ xorv;
-            spin_ballot(g, occ, rows + (size_t)slot * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
-          }
-        } else {
-          const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
-          int ib = (int)cemc_below(dr.w1, (uint32_t)(n_present - 1));
-          ib += (ib >= ia);
-          A_ = misc[4 + ia];
-          B_ = misc[4 + ib];
-          sa = trk[misc[12 + A_] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A_])];
-          sb = trk[misc[12 + B_] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B_])];
-          na = B_;
-          ua = dr.x0;
-          ub = dr.x1;
-          // first half: site a takes B; second half: site b takes A with a already changed
-          if (!SPIN) {
-            gather_vals<R>(g, occ, bf_s, sa, A_, B_, -1, 0, va, nbra, lane);
-            gather_vals<R>(g, occ, bf_s, sb, B_, A_, sa, B_, vb, nbrb, lane);
-          } else {
-            occ_a_bit = (uint32_t)A_ ^ xorv;
-            spin_ballot(g, occ, g.table + (size_t)sa * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
-            spin_ballot(g, occ, g.table + (size_t)sb * cpad, xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
-          }
-        }
-        R de;
-        int delta = 0;
-        if (!SPIN) {
-          __syncwarp();
-          lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
-          __syncwarp();
-          de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb, Dw, lane);
-          __syncwarp();
-        } else {
-          // P_k = sum over the terms of cluster ECI k of the product of the other
-          // members' spins; D_k = delta * P_k with delta = -2 s_a the spin change.
-          // Lane k evaluates cluster ECI k: its pair terms by popcounts of its shell
-          // masks, its multi-site terms from one warp reduction per ECI that has any.
-          delta = ((occ_a_bit) ? 2 : -2);
-          const int first = sp_first;
-          const uint32_t pa = spin_lane_parities(sp_masks, sp_shift, sp_tlo, sp_thi, wa_lo, wa_hi);
-          const uint32_t pb = SWAP ? spin_lane_parities(sp_masks, sp_shift, sp_tlo, sp_thi, wb_lo, wb_hi) : 0u;
-          int my_odd = 0;
-          for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
-            const int k = __ffs(mm) - 1;
-            const int sl = k - first;
-            int v = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
-            if (SWAP) v -= (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
-            const int odd = __reduce_add_sync(kFull, v);
-            if (lane == k) my_odd = odd;
-          }
-          int P = 0;
-          if (lane < sd.n_cl) {
-            if (!SWAP) {
-              P = sp_e.n_pairs - 2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi)) + sp_e.n_multi -
-                  2 * my_odd;
-            } else {
-              // P(a) - P(b after a): the term counts cancel
-              P = -2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi) - __popc(wb_lo & sp_e.pair_lo) -
-                        __popc(wb_hi & sp_e.pair_hi)) - 2 * my_odd;
-            }
-            Dw[sp_e.eci] = (R)(delta * P);
-          }
-          R sum = warp_sum(sp_coef * (R)P);
-          if (sd.singlet_eci >= 0) {
-            if (lane == 0) Dw[sd.singlet_eci] = (R)(SWAP ? 0 : delta);
-            if (!SWAP) sum += coef_s[sd.singlet_eci];
-          }
-          de = (R)delta * sum;
-        }
-        int acc = 0;
-        if (lane == 0) {
-          acc = metropolis<R>(de, ua, ub, kT, inv_kT);
-          put(&r_sa[gidx], (int32_t)sa);
-          put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
-          put(&r_acc[gidx], (int8_t)acc);
-          put(&r_de[gidx], de);
-          for (int b = 0; b < g.n_bf; ++b) {
-            R v = (R)0;
-            if (SPIN)
-              v = (R)(SWAP ? 0 : delta);
-            else if (g.singlet_eci[b] >= 0)
-              v = Dw[g.singlet_eci[b]];
-            put(&r_ds[b * kRoundSlots + gidx], v);
-          }
-          if (SWAP) {
-            put(&r_la[gidx], (int32_t)loc[sa]);
-            put(&r_lb[gidx], (int32_t)loc[sb]);
-            put(&r_A[gidx], (int8_t)A_);
-            put(&r_B[gidx], (int8_t)B_);
-          }
-        }
-        acc = __shfl_sync(kFull, acc, 0);
-        if (acc) {
-          const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (nbra[q] >= 0) {
-              uint32_t *p = &tab[(uint32_t)nbra[q] & hmask];
-              atomicMax(p, mark);
-              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
-            }
-            if (SWAP && nbrb[q] >= 0) {
-              uint32_t *p = &tab[(uint32_t)nbrb[q] & hmask];
-              atomicMax(p, mark);
-              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
-            }
-          }
-          if (lane == 0) {
-            uint32_t *p = &tab[(uint32_t)sa & hmask];
-            atomicMax(p, mark);
-            if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
-            if (SWAP) {
-              p = &tab[(uint32_t)sb & hmask];
-              atomicMax(p, mark);
-              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
-            }
-          }
-        }
-      }
-    } else if (booker) {
-      // ---- helpers: book the previous round; draw / prefetch ahead ----------------
-      if (round > 1) book(rec0 + (size_t)((round - 1) & 1) * L.rec_stride, ks_prev);
-    } else {
-      if (active) prefetch(t0);
-      cp_async_wait_prev();
-    }
+  // One round: every warp, whatever its role, meets the round barrier once and
+  // computes the same committed prefix `ks`, so the role loops below run in
+  // lockstep.  Returns false when the launch is over, or when a pair's round
+  // starts disagree (CEMC_ERR_INTERNAL, both CTAs stop at the same barrier).
+  auto end_round = [&](uint32_t round, uint64_t t0, bool active, int &ks) -> bool {
     if (CL == 2) {
       if (tid == 0) st_peer(peer_addr(&t0_slot[round & 1], peer), t0);
       cluster_barrier();
-      if (t0_slot[round & 1] != t0) {  // both CTAs see the same mismatch and stop together
+      if (t0_slot[round & 1] != t0) {
         if (tid == 0) misc[1] = CEMC_ERR_INTERNAL;
-        break;
+        return false;
       }
     } else {
       __syncthreads();
     }
-    if (!active) break;
-
-    // ---- phase B (every warp): the committed prefix, then its accepted moves ----
+    if (!active) return false;
+    const unsigned char *rec = rec0 + (size_t)(round & 1) * L.rec_stride;
+    const int32_t *r_sa = reinterpret_cast<const int32_t *>(rec + L.rec_sa);
+    const int32_t *r_sb = reinterpret_cast<const int32_t *>(rec + L.rec_sb);
+    const uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
     const int nv = (t_end - t0) < (uint64_t)CW ? (int)(t_end - t0) : CW;
     auto conflicted = [&](int gg) {
       const uint32_t v = tab[(uint32_t)r_sa[gg] & hmask];
@@ -770,49 +576,308 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     const bool c1 = lane + 32 < nv && conflicted(lane + 32);
     const unsigned m0 = __ballot_sync(kFull, c0);
     const unsigned m1 = __ballot_sync(kFull, c1);
-    const int ks = m0 ? (__ffs(m0) - 1) : (m1 ? (31 + __ffs(m1)) : nv);
-    if (!helper) {
-      for (int gg = lane; gg < ks; gg += 32) {
-        if (r_acc[gg]) {
-          const int sa = r_sa[gg];
+    ks = m0 ? (__ffs(m0) - 1) : (m1 ? (31 + __ffs(m1)) : nv);
+    return true;
+  };
+
+  uint64_t t0 = t_first;
+  uint32_t round = 1;
+  if (!helper) {
+    // ---- evaluating warps: speculate, then apply the committed prefix ----------
+    while (true) {
+      const bool active = t0 < t_end;
+      unsigned char *rec = rec0 + (size_t)(round & 1) * L.rec_stride;
+      int32_t *r_sa = reinterpret_cast<int32_t *>(rec + L.rec_sa);
+      int32_t *r_sb = reinterpret_cast<int32_t *>(rec + L.rec_sb);
+      int32_t *r_la = reinterpret_cast<int32_t *>(rec + L.rec_la);
+      int32_t *r_lb = reinterpret_cast<int32_t *>(rec + L.rec_lb);
+      int8_t *r_acc = reinterpret_cast<int8_t *>(rec + L.rec_acc);
+      int8_t *r_A = reinterpret_cast<int8_t *>(rec + L.rec_A);
+      int8_t *r_B = reinterpret_cast<int8_t *>(rec + L.rec_B);
+      R *r_de = reinterpret_cast<R *>(rec + L.rec_de);
+      R *r_ds = reinterpret_cast<R *>(rec + L.rec_ds);
+      uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
+      DT *dbuf = drow + (size_t)(round & 1) * TPW * W * n_eci;  // this round's change rows
+      DT *Dw = dbuf + (size_t)warp * n_eci;
+      if (TPW == 2) {
+        // ---- phase A, two flips per warp: half h = lane / 16 evaluates trial slot 2 warp + h ----
+        if (active && t0 + (uint64_t)(2 * warp) < t_end) {
+          const int h = lane >> 4, hl = lane & 15;
+          const int gh = 2 * warp + h;
+          const uint64_t t = t0 + (uint64_t)gh;
+          const bool has = t < t_end;  // the second half of the last warp may have no trial
+          const uint32_t slot = (uint32_t)t & rmask;
+          int sa = 0, na = 0, oa = 0;
+          uint32_t ua = 0, ub = 0;
+          if (has) {
+            const Draw dr = draws[slot];
+            sa = dr.site;
+            oa = occ[sa];
+            const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
+            na = k + (k >= oa);
+            ua = dr.w2;
+            ub = dr.w3;
+          }
+          const uint32_t occ_a_bit = (uint32_t)oa ^ xorv;
+          // spin word of the neighbour row: bit c = column c, from four ballots of
+          // 16 columns (c = hl + 16 j) of which each half keeps its own 16 bits
+          const int32_t *row = rows + (size_t)slot * cpad;
+          int nbr[4];
+          uint32_t wl = 0, wh = 0;
+  #pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int c = hl + 16 * j;
+            uint32_t bit = 0;
+            nbr[j] = -1;
+            if (has && c < g.n_cols) {
+              const int sn = row[c];
+              nbr[j] = sn;
+              bit = (uint32_t)occ[sn] ^ xorv;
+            }
+            const uint32_t chunk = (__ballot_sync(kFull, bit) >> (16 * h)) & 0xFFFFu;
+            if (j == 0) wl = chunk;
+            else if (j == 1) wl |= chunk << 16;
+            else if (j == 2) wh = chunk;
+            else wh |= chunk << 16;
+          }
+          const uint32_t pa = spin_lane_parities<true>(sp_terms, sp_tlo, sp_thi, wl, wh);
+          // odd-parity counts of each multi-site cluster ECI: one reduction serves
+          // both halves (half h's count in bits 16h .. 16h + 15, at most 16 x 63)
+          int my_odd = 0;
+          for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+            const int k = __ffs(mm) - 1;
+            const int sl = k - sp_first;
+            const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
+            const uint32_t tot = __reduce_add_sync(kFull, v << (16 * h));
+            if (hl == k) my_odd = (int)((tot >> (16 * h)) & 0xFFFFu);
+          }
+          const int delta = occ_a_bit ? 2 : -2;
+          DT *Dh = dbuf + (size_t)gh * n_eci;
+          int P = 0;
+          if (hl < sd.n_cl) {
+            P = sp_e.n_pairs - 2 * (__popc(wl & sp_e.pair_lo) + __popc(wh & sp_e.pair_hi)) + sp_e.n_multi - 2 * my_odd;
+            if (has) Dh[sp_e.eci] = delta * P;
+          }
+          R sum = sp_coef * (R)P;
+  #pragma unroll
+          for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+          if (sd.singlet_eci >= 0) {
+            if (hl == 0 && has) Dh[sd.singlet_eci] = delta;
+            sum += coef_s[sd.singlet_eci];
+          }
+          const R de = (R)delta * sum;
+          int acc = 0;
+          if (hl == 0 && has) {
+            acc = metropolis<R>(de, ua, ub, kT, inv_kT);
+            r_sa[gh] = sa;
+            r_sb[gh] = na;
+            r_acc[gh] = (int8_t)acc;
+            r_de[gh] = de;
+            r_ds[gh] = (R)delta;  // the singlet change (one decoration)
+          }
+          acc = __shfl_sync(kFull, acc, 16 * h);
+          if (acc) {
+            const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
+  #pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (nbr[j] >= 0) atomicMax(&tab[(uint32_t)nbr[j] & hmask], mark);
+            if (hl == 0) atomicMax(&tab[(uint32_t)sa & hmask], mark);
+          }
+        }
+      } else {
+        // ---- phase A: every evaluating warp computes one trial speculatively ----
+        const uint64_t t = t0 + (uint64_t)gidx;
+        if (active && t < t_end) {
+          const uint32_t slot = (uint32_t)t & rmask;
+          const Draw dr = draws[slot];
+          int sa, sb = -1, na, A_ = 0, B_ = 0;
+          int nbra[4], nbrb[4] = {-1, -1, -1, -1};
+          uint32_t ua, ub;
+          uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
           if (!SWAP) {
-            occ[sa] = (int8_t)r_sb[gg];
+            sa = dr.site;
+            const int oa = occ[sa];
+            const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
+            na = k + (k >= oa);
+            ua = dr.w2;
+            ub = dr.w3;
+            if (!SPIN) {
+              gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
+            } else {
+              occ_a_bit = (uint32_t)oa ^ xorv;
+              spin_ballot(g, occ, rows + (size_t)slot * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+            }
           } else {
-            const int sb = r_sb[gg], A_ = r_A[gg], B_ = r_B[gg], la = r_la[gg], lb = r_lb[gg];
-            occ[sa] = (int8_t)B_;
-            occ[sb] = (int8_t)A_;
-            trk[misc[12 + A_] + la] = sb;
-            loc[sb] = la;
-            trk[misc[12 + B_] + lb] = sa;
-            loc[sa] = lb;
+            const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
+            int ib = (int)cemc_below(dr.w1, (uint32_t)(n_present - 1));
+            ib += (ib >= ia);
+            A_ = misc[4 + ia];
+            B_ = misc[4 + ib];
+            sa = trk[misc[12 + A_] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A_])];
+            sb = trk[misc[12 + B_] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B_])];
+            na = B_;
+            ua = dr.x0;
+            ub = dr.x1;
+            // first half: site a takes B; second half: site b takes A with a already changed
+            if (!SPIN) {
+              gather_vals<R>(g, occ, bf_s, sa, A_, B_, -1, 0, va, nbra, lane);
+              gather_vals<R>(g, occ, bf_s, sb, B_, A_, sa, B_, vb, nbrb, lane);
+            } else {
+              occ_a_bit = (uint32_t)A_ ^ xorv;
+              spin_ballot(g, occ, g.table + (size_t)sa * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+              spin_ballot(g, occ, g.table + (size_t)sb * cpad, xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
+            }
+          }
+          R de;
+          int delta = 0;
+          if constexpr (!SPIN) {
+            __syncwarp();
+            lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
+            __syncwarp();
+            de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb, Dw, lane);
+            __syncwarp();
+          } else {
+            // P_k = sum over the terms of cluster ECI k of the product of the other
+            // members' spins; D_k = delta * P_k with delta = -2 s_a the spin change.
+            // Lane k evaluates cluster ECI k: its pair terms by popcounts of its shell
+            // masks, its multi-site terms from one warp reduction per ECI that has any.
+            delta = ((occ_a_bit) ? 2 : -2);
+            const int first = sp_first;
+            const uint32_t pa = spin_lane_parities<false>(sp_terms, sp_tlo, sp_thi, wa_lo, wa_hi);
+            const uint32_t pb = SWAP ? spin_lane_parities<false>(sp_terms, sp_tlo, sp_thi, wb_lo, wb_hi) : 0u;
+            int my_odd = 0;
+            for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+              const int k = __ffs(mm) - 1;
+              const int sl = k - first;
+              int v = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
+              if (SWAP) v -= (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
+              const int odd = __reduce_add_sync(kFull, v);
+              if (lane == k) my_odd = odd;
+            }
+            int P = 0;
+            if (lane < sd.n_cl) {
+              if (!SWAP) {
+                P = sp_e.n_pairs - 2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi)) + sp_e.n_multi -
+                    2 * my_odd;
+              } else {
+                // P(a) - P(b after a): the term counts cancel
+                P = -2 * (__popc(wa_lo & sp_e.pair_lo) + __popc(wa_hi & sp_e.pair_hi) - __popc(wb_lo & sp_e.pair_lo) -
+                          __popc(wb_hi & sp_e.pair_hi)) - 2 * my_odd;
+              }
+              Dw[sp_e.eci] = delta * P;
+            }
+            R sum = warp_sum(sp_coef * (R)P);
+            if (sd.singlet_eci >= 0) {
+              if (lane == 0) Dw[sd.singlet_eci] = SWAP ? 0 : delta;
+              if (!SWAP) sum += coef_s[sd.singlet_eci];
+            }
+            de = (R)delta * sum;
+          }
+          int acc = 0;
+          if (lane == 0) {
+            acc = metropolis<R>(de, ua, ub, kT, inv_kT);
+            put(&r_sa[gidx], (int32_t)sa);
+            put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
+            put(&r_acc[gidx], (int8_t)acc);
+            put(&r_de[gidx], de);
+            for (int b = 0; b < g.n_bf; ++b) {
+              R v = (R)0;
+              if constexpr (SPIN)
+                v = (R)(SWAP ? 0 : delta);
+              else if (g.singlet_eci[b] >= 0)
+                v = Dw[g.singlet_eci[b]];
+              put(&r_ds[b * kRoundSlots + gidx], v);
+            }
+            if (SWAP) {
+              put(&r_la[gidx], (int32_t)loc[sa]);
+              put(&r_lb[gidx], (int32_t)loc[sb]);
+              put(&r_A[gidx], (int8_t)A_);
+              put(&r_B[gidx], (int8_t)B_);
+            }
+          }
+          acc = __shfl_sync(kFull, acc, 0);
+          if (acc) {
+            const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
+  #pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if (nbra[q] >= 0) {
+                uint32_t *p = &tab[(uint32_t)nbra[q] & hmask];
+                atomicMax(p, mark);
+                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+              }
+              if (SWAP && nbrb[q] >= 0) {
+                uint32_t *p = &tab[(uint32_t)nbrb[q] & hmask];
+                atomicMax(p, mark);
+                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+              }
+            }
+            if (lane == 0) {
+              uint32_t *p = &tab[(uint32_t)sa & hmask];
+              atomicMax(p, mark);
+              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+              if (SWAP) {
+                p = &tab[(uint32_t)sb & hmask];
+                atomicMax(p, mark);
+                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+              }
+            }
           }
         }
       }
-      __syncwarp();
-#pragma unroll
-      for (int h2 = 0; h2 < TPW; ++h2) {
-        const int go = (TPW == 2) ? 2 * warp + h2 : gidx;  // this warp's trial slot(s)
-        if (go < ks) {
-          if (r_acc[go]) {
-            // this warp's committed accepted trial: add its change row to the warp's sums
-            const R *D = drow + (size_t)(TPW * warp + h2) * n_eci;
-            A *cw = cfw + (size_t)warp * n_eci;
-            for (int k = lane; k < n_eci; k += 32) cw[k] = acc_add_x(cw[k], D[k]);
-          }
-          if (a.trace_acc && lane == 0) {
-            const size_t idx = (size_t)chain * a.n_trials + (size_t)(t0 + go - t_first);
-            a.trace_site[2 * idx] = r_sa[go];
-            a.trace_site[2 * idx + 1] = r_sb[go];
-            a.trace_acc[idx] = r_acc[go];
-            a.trace_de[idx] = (double)r_de[go];
+      int ks;
+      if (!end_round(round, t0, active, ks)) break;
+      // ---- phase B: apply every accepted move of the committed prefix ----------
+      {
+        for (int gg = lane; gg < ks; gg += 32) {
+          if (r_acc[gg]) {
+            const int sa = r_sa[gg];
+            if (!SWAP) {
+              occ[sa] = (int8_t)r_sb[gg];
+            } else {
+              const int sb = r_sb[gg], A_ = r_A[gg], B_ = r_B[gg], la = r_la[gg], lb = r_lb[gg];
+              occ[sa] = (int8_t)B_;
+              occ[sb] = (int8_t)A_;
+              trk[misc[12 + A_] + la] = sb;
+              loc[sb] = la;
+              trk[misc[12 + B_] + lb] = sa;
+              loc[sa] = lb;
+            }
           }
         }
         __syncwarp();
       }
+      t0 += (uint64_t)ks;
+      ++round;
     }
-    ks_prev = ks;
-    t0 += (uint64_t)ks;
-    ++round;
+  } else if (booker) {
+    // ---- bookers: fold round r - 1 while round r is evaluated ------------------
+    int ks_prev = 0;
+    while (true) {
+      const bool active = t0 < t_end;
+      if (round > 1)
+        book(rec0 + (size_t)((round - 1) & 1) * L.rec_stride, drow + (size_t)((round - 1) & 1) * TPW * W * n_eci,
+             ks_prev, t0 - (uint64_t)ks_prev);
+      int ks;
+      if (!end_round(round, t0, active, ks)) break;
+      ks_prev = ks;
+      t0 += (uint64_t)ks;
+      ++round;
+    }
+    for (int i = 0; i < 4; ++i) {
+      const int k = lane + 32 * i;
+      if (k < n_eci) cfb[k] = cf_sum_out(cfr[i]);
+    }
+  } else {
+    // ---- fetcher: draws and neighbour rows kPrefetchRounds rounds ahead --------
+    while (true) {
+      const bool active = t0 < t_end;
+      if (active) prefetch(t0);
+      cp_async_wait_prev();
+      int ks;
+      if (!end_round(round, t0, active, ks)) break;
+      t0 += (uint64_t)ks;
+      ++round;
+    }
   }
 
   if (fetcher) cp_async_wait_all();
@@ -829,14 +894,13 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   double sum_v = 0.0;         // thread tid < NACC: running sum `tid` over the bookers' lanes
   uint64_t n_acc_total = 0;   // thread 0 of CTA 0: accepted trials of the launch
   if (rank == 0 && ok) {
-    // the launch's correlation-function changes: per-warp sums of both CTAs in
-    // warp order (exact for integer-valued changes), then one scaling per ECI
+    // the launch's correlation-function changes: the bookers' sums of both CTAs
+    // in fixed order (exact for integer-valued changes), then one scaling per ECI
     for (int k = tid; k < n_eci; k += blockDim.x) {
       const int kind = kind_s[k];
       double d = 0.0;
-      for (int w = 0; w < W; ++w) d += acc_to(cfw[(size_t)w * n_eci + k]);
-      if (CL == 2)
-        for (int w = 0; w < W; ++w) d += ld_peer_acc(&cfw[(size_t)w * n_eci + k], peer);
+      for (int q = 0; q < NB; ++q) d += acc_to(cfw[(size_t)q * n_eci + k]);
+      if (CL == 2) d += ld_peer_acc(&cfw[k], peer);
       if (kind == 2) cf_s[k] = cf_s[k] + d * w_s[k];
       else if (kind == 1) cf_s[k] = cf_s[k] + d / (double)N;
     }
