@@ -259,6 +259,117 @@ def run_served(args):
     return 0
 
 
+def _timed_steps(step, stream, steps: int, warmup: int, local: int):
+    """Device time of `steps` calls of step() after `warmup` untimed ones (CUDA events on `stream`)."""
+    import torch
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        a.record(stream)
+        for _ in range(steps):
+            step()
+        b.record(stream)
+        torch.cuda.synchronize()
+    return a.elapsed_time(b) * 1e-3, clk.summary()
+
+
+def run_ternary(args):
+    """Ternary canonical swaps on 256 chains of uneven supercells in one graph launch per step.
+
+    Ternary FCC {-1, 0, 1} (basis sqrt(3/2) s, sqrt(2)(1 - 1.5 s^2)), pairs to the 5th
+    shell, triplets to the 3rd, the nearest-neighbour tetrahedron; seeded ECIs; 256
+    chains on conventional cells L^3, L drawn uniformly from 4..24 (256..55296 sites);
+    compositions Dirichlet(2, 2, 2) per chain; T = 800 K; FP32 energy changes, FP64
+    recompute every step.  Chains of one size share a geometry; every size group runs
+    on its own stream inside one CUDA graph, so one graph launch steps all 256 chains.
+    """
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cemc_gb300 import engine as E
+    from cemc_gb300.batch import BatchRunner, MultiBatchRunner
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    rng = np.random.default_rng(1000 + rank)
+    sizes = rng.integers(4, 25, args.ternary_chains)
+    runners = []
+    for L in sorted(set(sizes.tolist())):
+        n = int((sizes == L).sum())
+        s = fcc_settings(int(L), 5, 3, 1, ["Al", "Mg", "Si"])
+        eci = seeded_ecis(s.cset, 0)
+        m = CEModel(s, list(eci))
+        geo = E.Geometry(m, dev)
+        occ = np.zeros((n, m.n_sites), dtype=np.int8)
+        for c in range(n):
+            comp = rng.dirichlet([2.0, 2.0, 2.0])
+            counts = np.floor(comp * m.n_sites).astype(int)
+            counts[0] += m.n_sites - counts.sum()
+            occ[c] = rng.permutation(np.repeat(np.arange(3), counts))
+        runners.append(BatchRunner(geo, occ, m.eci_vector(eci), 800.0, E.MOVE_SWAP, seed=7 + int(L),
+                                   precision=E.PREC_F32, warps=args.warps or 16, cluster=args.cluster,
+                                   sweeps_per_step=args.sweeps_per_step, recompute_every=1, graph=True,
+                                   chain_keys=np.arange(n) + 1000 * int(L)))
+    multi = MultiBatchRunner(runners)
+    multi.capture()
+    t, clocks = _timed_steps(multi.step, multi.stream, args.steps, args.warmup, local)
+    trials = float(multi.trials_per_step * args.steps)
+    for r in runners:
+        r.cb.check_status()
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload": "ternary_uneven", "value": trials / t, "unit": UNIT,
+                          "ms_per_step": t * 1e3 / args.steps, "steps": args.steps, "warmup": args.warmup,
+                          "dtype": "f32", "clocks": clocks,
+                          "config": {"workload": "ternary_swap_fcc_uneven_%dchains" % args.ternary_chains,
+                                     "n_chains": int(args.ternary_chains), "sizes": "L uniform 4..24",
+                                     "groups": len(runners), "sites_total": int(sum(r.n_chains * r.geo.n_sites
+                                                                                    for r in runners)),
+                                     "sweeps_per_step": args.sweeps_per_step, "warps_per_cta": args.warps or 16,
+                                     "launch": "one CUDA graph per step, one stream per supercell size"}}))
+    return 0
+
+
+def run_pt(args):
+    """Parallel-tempering ladder: binary FCC 32^3 (131072 sites), 48 replicas, exchange every 10 sweeps.
+
+    Cluster set: pairs to the 6th shell, triplets to the 2nd, the nearest-neighbour
+    tetrahedron; seeded ECIs; canonical swaps from a 50/50 random configuration;
+    geometric ladder T in [200, 1500] K; FP32 energy changes, FP64 recompute and
+    device exchange after every 10-sweep cycle.  One step = one cycle.
+    """
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cemc_gb300 import engine as E
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    from cemc_gb300.parallel_tempering import ParallelTempering
+    s = fcc_settings(32, 6, 2, 1, SPECIES)
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m, dev)
+    rng = np.random.default_rng(rank)
+    occ = np.zeros(m.n_sites, dtype=np.int8)
+    occ[rng.permutation(m.n_sites)[: m.n_sites // 2]] = 1
+    pt = ParallelTempering(geo, occ, m.eci_vector(eci), temperatures=np.geomspace(200.0, 1500.0, 48),
+                           move=E.MOVE_SWAP, seed=11, precision=E.PREC_F32, warps=args.warps or 0)
+    stream = torch.cuda.current_stream()
+    t, clocks = _timed_steps(lambda: pt.run(sweeps_per_cycle=10.0, num_exchange_cycles=1), stream, args.steps,
+                             args.warmup, local)
+    trials = 48.0 * 10 * m.n_sites * args.steps
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload": "parallel_tempering", "value": trials / t, "unit": UNIT,
+                          "ms_per_step": t * 1e3 / args.steps, "steps": args.steps, "warmup": args.warmup,
+                          "dtype": "f32", "clocks": clocks, "exchanges_accepted": int(pt.n_accept.item()),
+                          "config": {"workload": "pt_swap_fcc_binary_32x32x32_48replicas", "n_sites": m.n_sites,
+                                     "n_cols": m.n_cols, "replicas": 48, "T": "geometric 200..1500 K",
+                                     "sweeps_per_step": 10, "warps_per_cta": pt.warps}}))
+    return 0
+
+
 def run_recompute(args):
     """Full correlation-function recompute (cemc_recompute) alone, on the ladder geometry.
 
@@ -520,9 +631,11 @@ def main(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)
     p.add_argument("--no-correctness", action="store_true")
-    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served", "recompute"],
+    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served", "recompute", "ternary", "pt"],
                    help="sgc64: the headline 64-chain batch; served: the Poisson job stream; "
-                        "recompute: the full correlation-function recompute alone")
+                        "recompute: the full correlation-function recompute alone; ternary: 256 ternary "
+                        "chains of uneven size in one graph launch; pt: the 48-replica tempering ladder")
+    p.add_argument("--ternary-chains", type=int, default=256)
     p.add_argument("--recompute-cell", type=int, default=32)
     p.add_argument("--recompute-chains", type=int, default=48)
     p.add_argument("--served-jobs", type=int, default=300)
@@ -539,6 +652,10 @@ def main(argv=None):
         return run_served(args)
     if args.workload == "recompute":
         return run_recompute(args)
+    if args.workload == "ternary":
+        return run_ternary(args)
+    if args.workload == "pt":
+        return run_pt(args)
     return run_gpu(args)
 
 

@@ -27,6 +27,7 @@ KERNEL_AUTO = 0
 KERNEL_GENERIC = 1
 KERNEL_SPIN = 2
 KERNEL_SPIN_HALFWARP = 3
+KERNEL_TABLE = 4
 MAX_BF = 4
 
 _P = C.c_void_p
@@ -54,7 +55,8 @@ class RunDesc(C.Structure):
                 ("occ", _P), ("cf", _P), ("energy", _P), ("eci", _P), ("kT", _P), ("trial", _P), ("accum", _P),
                 ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
                 ("trace_site", _P), ("trace_acc", _P), ("trace_de", _P), ("status", _P), ("chain_key", _P),
-                ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32), ("cluster", C.c_int32)]
+                ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32), ("cluster", C.c_int32),
+                ("scratch", _P), ("scratch_doubles", C.c_uint64)]
 
 
 class CemcError(RuntimeError):

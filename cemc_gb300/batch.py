@@ -136,6 +136,72 @@ class BatchRunner:
         return out
 
 
+class MultiBatchRunner:
+    """Chains of several supercells stepped together: one CUDA graph per step.
+
+    Each group (one geometry and its chains) is a ``BatchRunner`` on its own
+    stream.  The captured step forks every group's stream from a capture stream,
+    records each group's MC launch and recompute on it, and joins them back, so
+    ONE graph launch runs all groups' kernels concurrently on the device (uneven
+    supercells do not wait for one another).  ``trials`` counts the step's
+    trials over all groups.
+    """
+
+    def __init__(self, runners: Sequence[BatchRunner]):
+        if not runners:
+            raise ValueError("no groups")
+        self.runners = list(runners)
+        self.device = self.runners[0].geo.device
+        self.stream = torch.cuda.Stream(device=self.device)
+        self._graph = None
+        self.trials_per_step = sum(r.n_chains * r.trials_per_step for r in self.runners)
+
+    @property
+    def n_chains(self) -> int:
+        return sum(r.n_chains for r in self.runners)
+
+    def _body(self):
+        start = torch.cuda.Event()
+        start.record(self.stream)
+        done = []
+        for r in self.runners:
+            r.stream.wait_event(start)
+            with torch.cuda.stream(r.stream):
+                r._step_body(r.recompute_every == 1)
+            ev = torch.cuda.Event()
+            ev.record(r.stream)
+            done.append(ev)
+        for ev in done:
+            self.stream.wait_event(ev)
+
+    def capture(self):
+        if self._graph is not None:
+            return
+        snaps = [r.snapshot() for r in self.runners]
+        with torch.cuda.stream(self.stream):
+            self._body()  # warm the launch path outside the capture
+        for r, snap in zip(self.runners, snaps):
+            r.restore(snap)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.stream):
+            self._body()
+        self._graph = g
+
+    def step(self, n: int = 1):
+        """Advance every chain of every group by ``n`` steps (asynchronous on the runner's stream)."""
+        if self._graph is None:
+            self.capture()
+        for _ in range(n):
+            with torch.cuda.stream(self.stream):
+                self._graph.replay()
+            for r in self.runners:
+                r.steps_done += 1
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+
 def sgc_grid(T_range=(300.0, 1200.0), mu_range=(-0.2, 0.2), n_T=8, n_mu=8):
     """Temperatures and chemical potentials of an n_T x n_mu semi-grand-canonical grid (T-major)."""
     Ts = np.repeat(np.linspace(T_range[0], T_range[1], n_T), n_mu)

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -155,6 +156,67 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
     }
     fterm_off[K] = T;
   }
+  // Table form of the trial energy change: the terms grouped by cluster geometry
+  // (the ordered member columns of a sub-cluster with the changed site as
+  // reference); geometries whose terms carry the same (ECI, decorations) list
+  // share a pattern, and each chain's kernel tabulates per pattern
+  // F(old, new, member species) = sum over its terms of coef * (bf[d_ref][new] -
+  // bf[d_ref][old]) * prod bf[d_j][s_j], so a flip costs one lookup per geometry.
+  std::vector<uint32_t> geo_list;  // per geometry: {packed columns, F offset, stride S^m, 0}
+  std::vector<int32_t> pat_info;   // per pattern: {m, F offset, first term, end term}
+  std::vector<int32_t> pat_terms;  // k | d_ref << 8 | d1 << 12 | d2 << 16 | d3 << 20
+  int n_geo = 0, n_pat = 0, tab_len = 0;
+  bool table_ok = C < 255 && S <= 8;
+  if (table_ok) {
+    std::map<std::vector<int>, std::vector<std::array<int, 5>>> geos;  // member columns -> terms
+    std::vector<std::vector<int>> geo_order;
+    for (int t = 0; t < T; ++t) {
+      const int m = d->term_size[t] - 1;
+      std::vector<int> cols(m);
+      std::array<int, 5> term{d->term_eci[t], d->term_ref[t], 0, 0, 0};
+      for (int j = 0; j < m; ++j) {
+        cols[j] = d->term_nb[3 * t + j] / B;
+        term[2 + j] = d->term_nb[3 * t + j] % B;
+      }
+      auto it = geos.find(cols);
+      if (it == geos.end()) {
+        geo_order.push_back(cols);
+        it = geos.emplace(cols, std::vector<std::array<int, 5>>{}).first;
+      }
+      it->second.push_back(term);
+    }
+    std::map<std::vector<std::array<int, 5>>, int> pats;
+    for (const auto &cols : geo_order) {
+      std::vector<std::array<int, 5>> sig = geos[cols];
+      std::sort(sig.begin(), sig.end());
+      const int m = (int)cols.size();
+      auto it = pats.find(sig);
+      if (it == pats.end()) {
+        int stride = 1;
+        for (int j = 0; j < m; ++j) stride *= S;
+        const int id = (int)pats.size();
+        it = pats.emplace(sig, id).first;
+        pat_info.insert(pat_info.end(), {m, tab_len, (int)pat_terms.size(), 0});
+        for (const auto &tm : sig)
+          pat_terms.push_back(tm[0] | (tm[1] << 8) | (tm[2] << 12) | (tm[3] << 16) | (tm[4] << 20));
+        pat_info[4 * id + 3] = (int)pat_terms.size();
+        tab_len += S * S * stride;
+      }
+      const int id = it->second;
+      uint32_t packed = 0;
+      for (int j = 0; j < 3; ++j) packed |= (uint32_t)(j < m ? cols[j] : C) << (8 * j);  // column C: species 0
+      int stride = 1;
+      for (int j = 0; j < m; ++j) stride *= S;
+      geo_list.insert(geo_list.end(), {packed, (uint32_t)pat_info[4 * id + 1], (uint32_t)stride, 0u});
+    }
+    n_geo = (int)geo_order.size();
+    n_pat = (int)pats.size();
+    if (tab_len > cemc::kMaxTable || n_geo > cemc::kMaxGeo) table_ok = false;
+  }
+  if (geo_list.empty()) geo_list.assign(4, 0u);
+  if (pat_info.empty()) pat_info.assign(4, 0);
+  if (pat_terms.empty()) pat_terms.assign(1, 0);
+
   // The trial kernel's conflict test needs a symmetric neighbour relation:
   // j in row(i) <=> i in row(j).
   {
@@ -281,6 +343,9 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {half_shift.data(), half_shift.size(), 0},
       {half_lane_term.data(), 17 * 4, 0},
       {half_lane_first.data(), 16 * 4, 0},
+      {geo_list.data(), geo_list.size() * 4, 0},
+      {pat_info.data(), pat_info.size() * 4, 0},
+      {pat_terms.data(), pat_terms.size() * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -327,6 +392,13 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.fterms = reinterpret_cast<const uint8_t *>(base + parts[11].off);
   g.fterm_off = reinterpret_cast<const int32_t *>(base + parts[12].off);
   for (int b = 0; b < CEMC_MAX_BF; ++b) g.singlet_eci[b] = singlet[b];
+  g.table_ok = table_ok ? 1 : 0;
+  g.n_geo = n_geo;
+  g.n_pat = n_pat;
+  g.tab_len = tab_len;
+  g.geo_list = reinterpret_cast<const uint4 *>(base + parts[21].off);
+  g.pat_info = reinterpret_cast<const int4 *>(base + parts[22].off);
+  g.pat_terms = reinterpret_cast<const int32_t *>(base + parts[23].off);
   g.pm1_minus = -1;
   if (B == 1 && S == 2) {
     if (d->bf[0] == 1.0 && d->bf[1] == -1.0) g.pm1_minus = 1;
@@ -376,13 +448,15 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     return fail(CEMC_ERR_ARG, "trace buffers must be given together");
   if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
   if (r->n_trials == 0) return CEMC_OK;
-  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_SPIN_HALFWARP)
+  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_TABLE)
     return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
   if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
   const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
   if (want_spin && !geo->spin_ok)
     return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
   const bool use_spin = want_spin || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
+  if (r->kernel == CEMC_KERNEL_TABLE && !g.table_ok)
+    return fail(CEMC_ERR_LIMIT, "the table kernel's pattern tables exceed %d entries", cemc::kMaxTable);
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
     return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs single-site flips with at most 16 cluster ECIs");
@@ -417,6 +491,18 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   a.chain_trials = r->chain_trials;
   a.tpw = tpw;
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
+  // Evaluation forms to try, in order: spin, or table then generic (AUTO), or the one asked for.
+  std::vector<int> forms;
+  if (use_spin)
+    forms = {cemc::kFormSpin};
+  else if (r->kernel == CEMC_KERNEL_TABLE)
+    forms = {cemc::kFormTable};
+  else if (r->kernel == CEMC_KERNEL_GENERIC)
+    forms = {cemc::kFormGeneric};
+  else if (g.table_ok)
+    forms = {cemc::kFormTable, cemc::kFormGeneric};
+  else
+    forms = {cemc::kFormGeneric};
   // Shared memory: the occupation, then (swaps) the site lists, then exact
   // stamp tables (one entry per site) are preferred; fall back in that order.
   const size_t budget = (size_t)geo->max_smem;
@@ -428,12 +514,13 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     int occ, trk, min_bits;
   };
   const Choice choices[] = {{1, is_swap, exact_bits}, {1, 0, exact_bits}, {1, 0, 12}, {0, 0, 12}, {0, 0, 5}};
+  int form = forms[0];
   auto fit = [&](int cl, cemc::McLayout &L, cemc::RunArgs &x) {
     const int w = std::min(warps, cemc::max_eval_warps(cl, tpw));
     const int rb = cemc::ring_bits_for(cemc::round_trials(cl, w, tpw));
     for (const Choice &ch : choices) {
       for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
-        L = cemc::mc_layout(g, w, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, use_spin, tpw);
+        L = cemc::mc_layout(g, w, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, form, tpw);
         if (L.total <= budget) {
           x.occ_smem = ch.occ;
           x.trk_smem = ch.trk;
@@ -449,33 +536,50 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   };
   // Resident cluster pairs of this configuration (cached per geometry).
   auto resident_pairs = [&](const cemc::McLayout &L, const cemc::RunArgs &x) {
-    const auto key = std::make_tuple(x.warps, (int)r->move, (int)r->precision, (int)use_spin, L.total);
+    const auto key = std::make_tuple(x.warps, (int)r->move, (int)r->precision, form, L.total);
     std::lock_guard<std::mutex> lock(geo->mu);
     auto it = geo->pairs.find(key);
     if (it != geo->pairs.end()) return it->second;
-    const int n = cemc::max_active_clusters(g, x, r->move, r->precision, L.total, use_spin);
+    const int n = cemc::max_active_clusters(g, x, r->move, r->precision, L.total, form);
     geo->pairs[key] = n;
     return n;
   };
   cemc::McLayout L{};
   bool found = false;
-  if (tpw == 1 && (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms))) {
-    cemc::RunArgs x = a;
-    cemc::McLayout L2{};
-    if (fit(2, L2, x)) {
-      const int n = resident_pairs(L2, x);
-      if (r->cluster == 2 && n < 1) return fail(CEMC_ERR_LIMIT, "no CTA pair of this size fits on the device");
-      if (r->cluster == 2 || n >= r->n_chains) {
-        a = x;
-        L = L2;
-        found = true;
+  for (size_t fi = 0; fi < forms.size() && !found; ++fi) {
+    form = forms[fi];
+    if (tpw == 1 && (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms))) {
+      cemc::RunArgs x = a;
+      cemc::McLayout L2{};
+      if (fit(2, L2, x)) {
+        const int n = resident_pairs(L2, x);
+        if (r->cluster == 2 && n < 1) return fail(CEMC_ERR_LIMIT, "no CTA pair of this size fits on the device");
+        if (r->cluster == 2 || n >= r->n_chains) {
+          a = x;
+          L = L2;
+          found = true;
+        }
+      } else if (r->cluster == 2 && fi + 1 == forms.size()) {
+        return fail(CEMC_ERR_LIMIT, "shared memory of a CTA pair exceeds %zu bytes; use fewer warps", budget);
       }
-    } else if (r->cluster == 2) {
-      return fail(CEMC_ERR_LIMIT, "shared memory of a CTA pair exceeds %zu bytes; use fewer warps", budget);
+    }
+    if (!found && r->cluster != 2) found = fit(1, L, a);
+  }
+  if (!found) return fail(CEMC_ERR_LIMIT, "shared memory exceeds %zu bytes; use fewer warps", budget);
+  // The table form leaves correlation functions to a full recompute at the end of the call.
+  double *rscratch = nullptr;
+  if (form == cemc::kFormTable) {
+    const size_t need = cemc::recompute_blocks(g) * (size_t)r->n_chains * (size_t)g.n_eci;
+    if (r->scratch && r->scratch_doubles >= need) {
+      rscratch = r->scratch;
+    } else if (need <= cemc::kNoAllocScratchDoubles) {
+      cudaError_t err = cudaSuccess;
+      rscratch = cemc::noalloc_scratch(&err);
+      if (!rscratch) return cuda_fail(err, "cudaGetSymbolAddress(recompute scratch)");
+    } else {
+      return fail(CEMC_ERR_LIMIT, "the table kernel needs a recompute scratch of %zu doubles (run desc scratch)", need);
     }
   }
-  if (!found) found = fit(1, L, a);
-  if (!found) return fail(CEMC_ERR_LIMIT, "shared memory exceeds %zu bytes; use fewer warps", budget);
   // Rounds are numbered in the upper 26 bits of the stamp marks: split very long runs.
   const uint64_t max_chunk = (uint64_t)1 << 25;
   if (r->n_trials > max_chunk && r->trace_acc)
@@ -484,10 +588,15 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     const uint64_t n = std::min(max_chunk, r->n_trials - done);
     a.n_trials = n;
     a.chunk_offset = done;
-    cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream),
+    cudaError_t e = cemc::launch_mc(g, a, r->move, r->precision, L.total, static_cast<cudaStream_t>(stream), form,
                                     use_spin ? &geo->spin : nullptr);
     if (e != cudaSuccess) return cuda_fail(e, "Monte Carlo kernel launch");
     done += n;
+  }
+  if (form == cemc::kFormTable) {
+    cudaError_t e = cemc::launch_recompute(g, r->n_chains, r->occ, r->eci, r->cf, r->energy, rscratch,
+                                           static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "recompute after the table kernel");
   }
   return CEMC_OK;
 }

@@ -13,6 +13,8 @@ constexpr int kMaxWarps = 32;
 constexpr int kMaxSlots = 31;      // ECIs one lane's chunk of terms may touch (5-bit field)
 constexpr int kRefBits = 11;       // low bits of a term's first field: vals index of the delta
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kMaxTable = 16384;   // table-form entries per chain (shared memory)
+constexpr int kMaxGeo = 2048;      // cluster geometries per site in the table form
 
 // Device copy of one geometry (supercell + cluster expansion).
 //
@@ -46,6 +48,11 @@ struct DevGeo {
   const int32_t *fterm_off; // [n_eci + 1] ranges of fterms per ECI
   int singlet_eci[CEMC_MAX_BF];
   int pm1_minus;  // binary basis with values exactly +1 / -1: species id of -1; otherwise -1
+  // table form of the trial energy change (see cemc_geometry_create)
+  int table_ok, n_geo, n_pat, tab_len;
+  const uint4 *geo_list;     // [n_geo] {columns c1 | c2 << 8 | c3 << 16 (absent: n_cols), F offset, S^m, 0}
+  const int4 *pat_info;      // [n_pat] {m, F offset, first term, end term}
+  const int32_t *pat_terms;  // k | d_ref << 8 | d1 << 12 | d2 << 16 | d3 << 20
 };
 
 __device__ __forceinline__ double warp_sum(double v) {

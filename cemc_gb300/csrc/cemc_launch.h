@@ -63,6 +63,7 @@ struct McLayout {
   // per-round trial records (two buffers, by round parity), kRoundSlots entries each
   size_t rec, rec_stride, rec_sa, rec_sb, rec_de, rec_ds, rec_acc, rec_la, rec_lb, rec_A, rec_B;
   size_t drow;  // [2][warps * tpw][n_eci] correlation-function changes of this CTA's trials
+  size_t ftab, geos;  // table form
   size_t draws, rows;
   size_t warp0, warp_stride, warp_part;
   size_t occ, trk, stamp;
@@ -73,9 +74,15 @@ struct McLayout {
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // Shared-memory carve-up of mc_kernel for `warps` evaluating warps per CTA.
+// Trial-evaluation forms of the kernel.
+constexpr int kFormGeneric = 0;  // basis-function products term by term; tracks correlation functions
+constexpr int kFormSpin = 1;     // binary +1/-1 basis: bit-packed neighbourhoods
+constexpr int kFormTable = 2;    // one lookup per cluster geometry; correlation functions by a final recompute
+
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
                                               int trk_smem, int stamp_bits, int n_cl, int n_masks, int ring_bits,
-                                              bool spin, int tpw) {
+                                              int form, int tpw) {
+  const bool spin = form == kFormSpin, table = form == kFormTable;
   McLayout L;
   size_t o = 0;
   const size_t K = (size_t)g.n_eci;
@@ -131,8 +138,12 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   L.rec_stride = align16(r);
   L.rec = o;
   o = align16(o + 2 * L.rec_stride);
-  L.drow = o;  // two buffers (round parity) of [warps * tpw][n_eci]
-  o = align16(o + 2 * (size_t)rsize * warps * tpw * K);
+  L.drow = o;  // two buffers (round parity) of [warps * tpw][n_eci] (none in the table form)
+  if (!table) o = align16(o + 2 * (size_t)rsize * warps * tpw * K);
+  L.ftab = o;  // table form: per-chain pattern tables F, then the geometry list
+  if (table) o = align16(o + (size_t)rsize * g.tab_len);
+  L.geos = o;
+  if (table) o = align16(o + 16 * (size_t)g.n_geo);
   const size_t ring = (size_t)1 << ring_bits;
   L.draws = o;
   o = align16(o + sizeof(Draw) * ring);
@@ -141,6 +152,7 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   const size_t vals = (size_t)rsize * g.vals_len * (move == CEMC_MOVE_SWAP ? 2 : 1);
   L.warp_part = align16(vals);
   L.warp_stride = spin ? 0 : align16(L.warp_part + (size_t)rsize * g.n_slots * 32);
+  if (table) L.warp_stride = 2 * align16((size_t)g.n_cols + 1);  // species of the two rows of a trial
   L.warp0 = o;
   o = align16(o + L.warp_stride * (size_t)warps);
   L.stamp_bits = stamp_bits;
@@ -156,8 +168,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
 
 struct SpinDev;
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
-                      const SpinDev *spin);
+                      int form, const SpinDev *spin);
 // Clusters of `cl` CTAs (each with `smem` bytes) that can be resident at once; 0 if none.
-int max_active_clusters(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, bool spin);
+int max_active_clusters(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, int form);
 
 }  // namespace cemc

@@ -127,6 +127,41 @@ __device__ __forceinline__ uint32_t spin_lane_parities(const uint4 *terms, int l
 
 
 
+// ---- table form ---------------------------------------------------------------
+// Species of the neighbour columns of `row` into sp[0..n_cols) (site `ovr` read
+// as species `ovr_s`); each lane keeps the site ids of its columns in nbr[] for
+// the conflict stamps.
+__device__ __forceinline__ void table_gather(const DevGeo &g, const int8_t *occ, const int32_t *row, int ovr,
+                                             int ovr_s, int8_t *sp, int (&nbr)[4], int lane) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = lane + 32 * j;
+    nbr[j] = -1;
+    if (c < g.n_cols) {
+      const int s = row[c];
+      nbr[j] = s;
+      sp[c] = (int8_t)(s == ovr ? ovr_s : occ[s]);
+    }
+  }
+}
+
+// Energy change of one flip (or, TWO, of a swap's two flips) from the pattern
+// tables: one lookup per cluster geometry, F[off + on * S^m + s1 + S s2 + S^2 s3]
+// with on = old * S + new and the member species s_j of the geometry's columns.
+template <typename R, bool TWO>
+__device__ __forceinline__ R table_de(const DevGeo &g, const uint4 *geos, const R *F, const int8_t *spa,
+                                      const int8_t *spb, int on_a, int on_b, int lane) {
+  const int S = g.n_sym, S2 = S * S;
+  R sum = (R)0;
+  for (int i = lane; i < g.n_geo; i += 32) {
+    const uint4 e = geos[i];
+    const int c1 = e.x & 0xff, c2 = (e.x >> 8) & 0xff, c3 = (e.x >> 16) & 0xff;
+    sum += F[e.y + on_a * e.z + spa[c1] + S * spa[c2] + S2 * spa[c3]];
+    if (TWO) sum += F[e.y + on_b * e.z + spb[c1] + S * spb[c2] + S2 * spb[c3]];
+  }
+  return warp_sum(sum);
+}
+
 // ---- thread-block cluster pairs ---------------------------------------------
 __device__ __forceinline__ unsigned cluster_cta_rank() {
   unsigned r;
@@ -175,15 +210,16 @@ __device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
   return (double)hi + (double)lo;
 }
 
-template <typename R, int MOVE, bool SPIN, int CL, int TPW>
+template <typename R, int MOVE, int FORM, int CL, int TPW>
 __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
+  constexpr bool SPIN = (FORM == kFormSpin), TAB = (FORM == kFormTable);
   const int W = a.warps;   // evaluating warps per CTA, then NB booker warps and one fetcher warp
   const int CW = round_trials(CL, W, TPW);  // trials per round
   const int NB = n_bookers(CL, W, TPW);
   const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits, SPIN ? sd.n_cl : 0,
-                               SPIN ? sd.n_masks : 0, a.ring_bits, SPIN, TPW);
+                               SPIN ? sd.n_masks : 0, a.ring_bits, FORM, TPW);
   const uint32_t rmask = (1u << a.ring_bits) - 1u;
   const int rank = (CL == 2) ? (int)cluster_cta_rank() : 0;
   const unsigned peer = (unsigned)(rank ^ 1);
@@ -237,6 +273,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   DT *drow = reinterpret_cast<DT *>(smem + L.drow);
   unsigned char *wbase = smem + L.warp0 + (size_t)(helper ? 0 : warp) * L.warp_stride;
   R *va = reinterpret_cast<R *>(wbase);
+  int8_t *sp_a = reinterpret_cast<int8_t *>(wbase);  // table form: species of the trial's rows
+  int8_t *sp_b = sp_a + align16((size_t)g.n_cols + 1);
+  R *ftab = reinterpret_cast<R *>(smem + L.ftab);
+  uint4 *geos_s = reinterpret_cast<uint4 *>(smem + L.geos);
   R *vb = va + g.vals_len;
   R *part = reinterpret_cast<R *>(wbase + L.warp_part);
 
@@ -278,8 +318,41 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
   for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
   for (int i = tid; i < 2 * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
-  for (int i = tid; i < 2 * TPW * W * n_eci; i += blockDim.x)
-    drow[i] = (DT)0;  // the spin path writes only the entries of cluster and singlet ECIs
+  if (!TAB)
+    for (int i = tid; i < 2 * TPW * W * n_eci; i += blockDim.x)
+      drow[i] = (DT)0;  // the spin path writes only the entries of cluster and singlet ECIs
+  if (TAB) {
+    // this chain's pattern tables F(old, new, member species), in FP64 then rounded to R
+    const int S = g.n_sym;
+    for (int i = tid; i < g.n_geo; i += blockDim.x) geos_s[i] = g.geo_list[i];
+    for (int idx = tid; idx < g.tab_len; idx += blockDim.x) {
+      int p = 0;
+      while (p + 1 < g.n_pat && g.pat_info[p + 1].y <= idx) ++p;
+      const int4 pi = g.pat_info[p];
+      int stride = 1;
+      for (int j = 0; j < pi.x; ++j) stride *= S;
+      const int li = idx - pi.y, on = li / stride, tup = li - on * stride;
+      const int old_s = on / S, new_s = on - old_s * S;
+      double v = 0.0;
+      for (int t = pi.z; t < pi.w; ++t) {
+        const int pk = g.pat_terms[t];
+        const int k = pk & 0xff, dr = (pk >> 8) & 15;
+        double prod = g.bf[dr * S + new_s] - g.bf[dr * S + old_s];
+        int tt = tup;
+        for (int j = 0; j < pi.x; ++j) {
+          const int sj = tt % S;
+          tt /= S;
+          prod *= g.bf[((pk >> (12 + 4 * j)) & 15) * S + sj];
+        }
+        v += a.eci[(size_t)chain * n_eci + k] * (double)N * g.eci_w[k] * prod;
+      }
+      ftab[idx] = (R)v;
+    }
+    if (!helper && lane == 0) {
+      sp_a[g.n_cols] = 0;  // the absent member of a smaller cluster reads species 0
+      sp_b[g.n_cols] = 0;
+    }
+  }
   for (int i = tid; i < 2 * NACC * 32; i += blockDim.x) lacc0[i] = acc_from<A>(0.0);
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
@@ -499,7 +572,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       carry_half(rec, 0, k0);
       if (k1 > 0) book_half(rec, 32, k1, tb);
     }
-    book_cf(rec, dbuf, ks);
+    if constexpr (!TAB) book_cf(rec, dbuf, ks);  // the table form leaves the CFs to a recompute
   };
 
   // Store into this CTA's shared memory and, in a pair, the peer's copy.
@@ -690,7 +763,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         if (active && t < t_end) {
           const uint32_t slot = (uint32_t)t & rmask;
           const Draw dr = draws[slot];
-          int sa, sb = -1, na, A_ = 0, B_ = 0;
+          int sa, sb = -1, na, A_ = 0, B_ = 0, old_a = 0;
           int nbra[4], nbrb[4] = {-1, -1, -1, -1};
           uint32_t ua, ub;
           uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
@@ -701,7 +774,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             na = k + (k >= oa);
             ua = dr.w2;
             ub = dr.w3;
-            if (!SPIN) {
+            old_a = oa;
+            if constexpr (TAB) {
+              table_gather(g, occ, rows + (size_t)slot * cpad, -1, 0, sp_a, nbra, lane);
+            } else if constexpr (!SPIN) {
               gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
             } else {
               occ_a_bit = (uint32_t)oa ^ xorv;
@@ -719,7 +795,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             ua = dr.x0;
             ub = dr.x1;
             // first half: site a takes B; second half: site b takes A with a already changed
-            if (!SPIN) {
+            if constexpr (TAB) {
+              table_gather(g, occ, g.table + (size_t)sa * cpad, -1, 0, sp_a, nbra, lane);
+              table_gather(g, occ, g.table + (size_t)sb * cpad, sa, B_, sp_b, nbrb, lane);
+            } else if constexpr (!SPIN) {
               gather_vals<R>(g, occ, bf_s, sa, A_, B_, -1, 0, va, nbra, lane);
               gather_vals<R>(g, occ, bf_s, sb, B_, A_, sa, B_, vb, nbrb, lane);
             } else {
@@ -730,7 +809,19 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           }
           R de;
           int delta = 0;
-          if constexpr (!SPIN) {
+          if constexpr (TAB) {
+            __syncwarp();
+            const int S = g.n_sym;
+            if (!SWAP) {
+              de = table_de<R, false>(g, geos_s, ftab, sp_a, sp_b, old_a * S + na, 0, lane);
+              for (int b = 0; b < g.n_bf; ++b)
+                if (g.singlet_eci[b] >= 0)
+                  de += coef_s[g.singlet_eci[b]] * (bf_s[b * S + na] - bf_s[b * S + old_a]);
+            } else {
+              de = table_de<R, true>(g, geos_s, ftab, sp_a, sp_b, A_ * S + B_, B_ * S + A_, lane);
+            }
+            __syncwarp();
+          } else if constexpr (!SPIN) {
             __syncwarp();
             lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
             __syncwarp();
@@ -784,6 +875,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
               R v = (R)0;
               if constexpr (SPIN)
                 v = (R)(SWAP ? 0 : delta);
+              else if constexpr (TAB)
+                v = SWAP ? (R)0 : bf_s[b * g.n_sym + na] - bf_s[b * g.n_sym + old_a];
               else if (g.singlet_eci[b] >= 0)
                 v = Dw[g.singlet_eci[b]];
               put(&r_ds[b * kRoundSlots + gidx], v);
@@ -965,9 +1058,9 @@ static unsigned block_threads(const RunArgs &a) {
   return (unsigned)((a.warps + n_bookers(a.cl, a.warps, a.tpw) + 1) * 32);
 }
 
-template <typename R, int MOVE, bool SPIN, int CL, int TPW>
+template <typename R, int MOVE, int FORM, int CL, int TPW>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
-  auto k = mc_kernel<R, MOVE, SPIN, CL, TPW>;
+  auto k = mc_kernel<R, MOVE, FORM, CL, TPW>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
@@ -987,9 +1080,9 @@ static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cuda
   return cudaGetLastError();
 }
 
-template <typename R, int MOVE, bool SPIN>
+template <typename R, int MOVE, int FORM>
 static int clusters_t(const RunArgs &a, size_t smem) {
-  auto k = mc_kernel<R, MOVE, SPIN, 2, 1>;
+  auto k = mc_kernel<R, MOVE, FORM, 2, 1>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_chains * 2));
@@ -1010,41 +1103,47 @@ static int clusters_t(const RunArgs &a, size_t smem) {
   return n;
 }
 
+template <typename R, int MOVE, int FORM>
+static cudaError_t launch_f(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
+  return a.cl == 2 ? launch_t<R, MOVE, FORM, 2, 1>(g, a, smem, st, sd) : launch_t<R, MOVE, FORM, 1, 1>(g, a, smem, st, sd);
+}
+
 template <typename R>
-static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t smem, cudaStream_t st,
+static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t smem, cudaStream_t st, int form,
                             const SpinDev *spin) {
   const SpinDev none{};
   if (move == CEMC_MOVE_SWAP) {
-    if (spin) return a.cl == 2 ? launch_t<R, CEMC_MOVE_SWAP, true, 2, 1>(g, a, smem, st, *spin)
-                               : launch_t<R, CEMC_MOVE_SWAP, true, 1, 1>(g, a, smem, st, *spin);
-    return a.cl == 2 ? launch_t<R, CEMC_MOVE_SWAP, false, 2, 1>(g, a, smem, st, none)
-                     : launch_t<R, CEMC_MOVE_SWAP, false, 1, 1>(g, a, smem, st, none);
+    if (form == kFormSpin) return launch_f<R, CEMC_MOVE_SWAP, kFormSpin>(g, a, smem, st, *spin);
+    if (form == kFormTable) return launch_f<R, CEMC_MOVE_SWAP, kFormTable>(g, a, smem, st, none);
+    return launch_f<R, CEMC_MOVE_SWAP, kFormGeneric>(g, a, smem, st, none);
   }
-  if (spin) {
-    if (a.tpw == 2) return launch_t<R, CEMC_MOVE_FLIP, true, 1, 2>(g, a, smem, st, *spin);
-    return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, true, 2, 1>(g, a, smem, st, *spin)
-                     : launch_t<R, CEMC_MOVE_FLIP, true, 1, 1>(g, a, smem, st, *spin);
+  if (form == kFormSpin) {
+    if (a.tpw == 2) return launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 1, 2>(g, a, smem, st, *spin);
+    return launch_f<R, CEMC_MOVE_FLIP, kFormSpin>(g, a, smem, st, *spin);
   }
-  return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, false, 2, 1>(g, a, smem, st, none)
-                   : launch_t<R, CEMC_MOVE_FLIP, false, 1, 1>(g, a, smem, st, none);
+  if (form == kFormTable) return launch_f<R, CEMC_MOVE_FLIP, kFormTable>(g, a, smem, st, none);
+  return launch_f<R, CEMC_MOVE_FLIP, kFormGeneric>(g, a, smem, st, none);
 }
 
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
-                      const SpinDev *spin) {
+                      int form, const SpinDev *spin) {
   // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
-  if (a.tpw == 2 && (!spin || move != CEMC_MOVE_FLIP || a.cl != 1)) return cudaErrorInvalidValue;
-  return precision == CEMC_PREC_F32 ? launch_r<float>(g, a, move, smem, st, spin)
-                                    : launch_r<double>(g, a, move, smem, st, spin);
+  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP || a.cl != 1)) return cudaErrorInvalidValue;
+  if (form == kFormSpin && !spin) return cudaErrorInvalidValue;
+  return precision == CEMC_PREC_F32 ? launch_r<float>(g, a, move, smem, st, form, spin)
+                                    : launch_r<double>(g, a, move, smem, st, form, spin);
 }
 
-int max_active_clusters(const DevGeo &, const RunArgs &a, int move, int precision, size_t smem, bool spin) {
-  const bool f32 = precision == CEMC_PREC_F32, swap = move == CEMC_MOVE_SWAP;
-  if (spin) {
-    if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, true>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, true>(a, smem);
-    return swap ? clusters_t<double, CEMC_MOVE_SWAP, true>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, true>(a, smem);
-  }
-  if (f32) return swap ? clusters_t<float, CEMC_MOVE_SWAP, false>(a, smem) : clusters_t<float, CEMC_MOVE_FLIP, false>(a, smem);
-  return swap ? clusters_t<double, CEMC_MOVE_SWAP, false>(a, smem) : clusters_t<double, CEMC_MOVE_FLIP, false>(a, smem);
+template <typename R, int FORM>
+static int clusters_m(const RunArgs &a, int move, size_t smem) {
+  return move == CEMC_MOVE_SWAP ? clusters_t<R, CEMC_MOVE_SWAP, FORM>(a, smem) : clusters_t<R, CEMC_MOVE_FLIP, FORM>(a, smem);
+}
+
+int max_active_clusters(const DevGeo &, const RunArgs &a, int move, int precision, size_t smem, int form) {
+  const bool f32 = precision == CEMC_PREC_F32;
+  if (form == kFormSpin) return f32 ? clusters_m<float, kFormSpin>(a, move, smem) : clusters_m<double, kFormSpin>(a, move, smem);
+  if (form == kFormTable) return f32 ? clusters_m<float, kFormTable>(a, move, smem) : clusters_m<double, kFormTable>(a, move, smem);
+  return f32 ? clusters_m<float, kFormGeneric>(a, move, smem) : clusters_m<double, kFormGeneric>(a, move, smem);
 }
 
 }  // namespace cemc

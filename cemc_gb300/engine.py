@@ -26,6 +26,7 @@ KERNEL_AUTO = _lib.KERNEL_AUTO
 KERNEL_GENERIC = _lib.KERNEL_GENERIC
 KERNEL_SPIN = _lib.KERNEL_SPIN
 KERNEL_SPIN_HALFWARP = _lib.KERNEL_SPIN_HALFWARP
+KERNEL_TABLE = _lib.KERNEL_TABLE
 ACCUM_DOUBLES = _lib.ACCUM_DOUBLES
 # Field offsets (in doubles) of cemc_accum.
 A_EREF, A_SUM_E, A_SUM_E2, A_SUM_S, A_SUM_S2, A_SUM_SE, A_NSAMP, A_NACC = 0, 1, 2, 3, 7, 11, 15, 16
@@ -243,7 +244,7 @@ class ChainBatch:
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
-                         _ptr(chain_trials), int(kernel), int(cluster))
+                         _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel())
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         if trace:

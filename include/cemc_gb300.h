@@ -136,21 +136,29 @@ typedef struct {
   int32_t kernel;      /* CEMC_KERNEL_*: which implementation runs the trials */
   int32_t cluster;     /* CTAs per chain: 1, 2 (a thread-block cluster pair on two SMs, twice the trials
                           per round), or 0 = 2 when every chain's pair fits on the GPU at once, else 1 */
+  double *scratch;     /* table kernel: buffer for the final recompute (cemc_recompute_scratch_doubles()
+                          doubles); NULL = the library's fixed array when it is large enough */
+  uint64_t scratch_doubles;
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when
  * the geometry allows it (two species with basis values +1 and -1, at most 64
- * neighbour columns, at most 32 cluster ECIs), else the generic one; for
- * single-site flips with at most 16 cluster ECIs and no CTA pair asked for it
- * takes the half-warp spin form.  All give the same decisions for the same
- * stream.  The spin forms evaluate a trial from a bit-packed neighbourhood
- * (popcounts of shell masks, parities of multi-site terms), one trial per warp
- * or, half-warp form, one per 16 lanes; the generic form multiplies basis
- * values term by term. */
+ * neighbour columns, at most 32 cluster ECIs) — the half-warp spin form for
+ * single-site flips with at most 16 cluster ECIs when no CTA pair is asked
+ * for — else the table form when its tables fit, else the generic form.  All
+ * give the same decisions for the same stream.  The spin forms evaluate a
+ * trial from a bit-packed neighbourhood (popcounts of shell masks, parities of
+ * multi-site terms), one trial per warp or one per 16 lanes; the generic form
+ * multiplies basis values term by term and keeps the correlation functions up
+ * to date trial by trial; the table form looks up one precomputed energy change
+ * per cluster geometry (tables built per chain from its ECIs at launch) and
+ * brings correlation functions and energies up to date with a full recompute
+ * at the end of the call (run desc `scratch`). */
 #define CEMC_KERNEL_AUTO 0
 #define CEMC_KERNEL_GENERIC 1
 #define CEMC_KERNEL_SPIN 2
 #define CEMC_KERNEL_SPIN_HALFWARP 3  /* spin basis, flips only, two trials per warp (one per 16 lanes) */
+#define CEMC_KERNEL_TABLE 4  /* one table lookup per cluster geometry; CFs and energies by a final recompute */
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
  * energy change, accept test and in-place commit of occupation, correlation

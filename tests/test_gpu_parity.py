@@ -61,7 +61,7 @@ def _kernel_ok(m, kernel, E, move=0, cluster=0):
         pytest.skip("the half-warp spin kernel runs flips on one CTA per chain")
 
 
-KERNELS = [1, 2, 3]  # generic, spin, spin half-warp
+KERNELS = [1, 2, 3, 4]  # generic, spin, spin half-warp, table
 CLUSTERS = [1, 2]  # CTAs per chain
 
 
