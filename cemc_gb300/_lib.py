@@ -56,7 +56,8 @@ class RunDesc(C.Structure):
                 ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
                 ("trace_site", _P), ("trace_acc", _P), ("trace_de", _P), ("status", _P), ("chain_key", _P),
                 ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32), ("cluster", C.c_int32),
-                ("scratch", _P), ("scratch_doubles", C.c_uint64)]
+                ("scratch", _P), ("scratch_doubles", C.c_uint64), ("stamps", _P), ("stamp_words", C.c_uint64),
+                ("kernel_used", C.c_int32)]
 
 
 class CemcError(RuntimeError):
@@ -94,6 +95,8 @@ def load():
         L.cemc_recompute_scratch_doubles.restype = C.c_size_t
         L.cemc_recompute_scratch_doubles.argtypes = [_P, C.c_int32]
         L.cemc_recompute.argtypes = [_P, C.c_int32, _P, _P, _P, _P, _P, _P]
+        L.cemc_stamp_words.restype = C.c_size_t
+        L.cemc_stamp_words.argtypes = [_P, C.c_int32]
         L.cemc_energy.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
         L.cemc_recompute_noalloc.argtypes = [_P, C.c_int32, _P, _P, _P, _P, _P]
         L.cemc_apply_changes.argtypes = [_P, _P, _P, _P, _P, C.c_int32, _P, _P, _P, _P, _P]
@@ -121,7 +124,7 @@ def exported_symbols():
     L = load()
     names = []
     for n in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_run", "cemc_recompute_scratch_doubles",
-              "cemc_recompute", "cemc_recompute_noalloc", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
+              "cemc_stamp_words", "cemc_recompute", "cemc_recompute_noalloc", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
               "cemc_version"):
         if hasattr(L, n):
             names.append(n)

@@ -53,7 +53,7 @@ class BatchRunner:
 
     def _step_body(self, with_recompute: bool):
         self.cb.run(self.trials_per_step, precision=self.precision, warps=self.warps, cluster=self.cluster)
-        if with_recompute:
+        if with_recompute and not self.cb.recomputed:
             self.cb.recompute()
 
     def capture(self):

@@ -434,7 +434,14 @@ extern "C" int cemc_geometry_destroy(cemc_geometry *geo) {
   return CEMC_OK;
 }
 
-extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *stream) {
+extern "C" size_t cemc_stamp_words(const cemc_geometry *geo, int32_t n_chains) {
+  if (!geo || n_chains <= 0) return 0;
+  int bits = 5;
+  while ((1 << bits) < geo->g.n_sites) ++bits;
+  return 2 * ((size_t)1 << bits) * (size_t)n_chains;
+}
+
+extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream) {
   if (!geo || !r) return fail(CEMC_ERR_ARG, "null geometry or run descriptor");
   const cemc::DevGeo &g = geo->g;
   if (r->n_chains <= 0) return fail(CEMC_ERR_ARG, "no chains");
@@ -447,6 +454,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   if ((r->trace_site || r->trace_acc || r->trace_de) && !(r->trace_site && r->trace_acc && r->trace_de))
     return fail(CEMC_ERR_ARG, "trace buffers must be given together");
   if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
+  r->kernel_used = CEMC_KERNEL_AUTO;  // nothing launched yet
   if (r->n_trials == 0) return CEMC_OK;
   if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_TABLE)
     return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
@@ -467,7 +475,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
                                                                 r->cluster != 2)) ? 2 : 1;
   int warps = r->warps > 0 ? r->warps : 16;
   const int rsize = r->precision == CEMC_PREC_F32 ? 4 : 8;
-  cemc::RunArgs a;
+  cemc::RunArgs a{};
   a.n_chains = r->n_chains;
   a.warps = warps;
   a.seed = r->seed;
@@ -511,20 +519,27 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
   if (exact_bits < 5) exact_bits = 5;
   const int is_swap = r->move == CEMC_MOVE_SWAP;
   struct Choice {
-    int occ, trk, min_bits;
+    int occ, trk, min_bits, global;
   };
-  const Choice choices[] = {{1, is_swap, exact_bits}, {1, 0, exact_bits}, {1, 0, 12}, {0, 0, 12}, {0, 0, 5}};
+  // exact tables in a caller buffer come before hashed shared-memory ones (hashing only costs speed)
+  const bool gbuf = r->stamps && r->stamp_words >= cemc_stamp_words(geo, r->n_chains);
+  std::vector<Choice> choices = {{1, is_swap, exact_bits, 0}, {1, 0, exact_bits, 0}};
+  if (gbuf) choices.insert(choices.end(), {{1, is_swap, exact_bits, 1}, {1, 0, exact_bits, 1}});
+  choices.insert(choices.end(), {{1, 0, 12, 0}, {0, 0, 12, 0}});
+  if (gbuf) choices.push_back({0, 0, exact_bits, 1});
+  choices.push_back({0, 0, 5, 0});
   int form = forms[0];
   auto fit = [&](int cl, cemc::McLayout &L, cemc::RunArgs &x) {
     const int w = std::min(warps, cemc::max_eval_warps(cl, tpw));
     const int rb = cemc::ring_bits_for(cemc::round_trials(cl, w, tpw));
     for (const Choice &ch : choices) {
       for (int bits = exact_bits; bits >= std::min(ch.min_bits, exact_bits); --bits) {
-        L = cemc::mc_layout(g, w, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, form, tpw);
+        L = cemc::mc_layout(g, w, r->move, rsize, ch.occ, ch.trk, bits, n_cl, n_masks, rb, form, tpw, ch.global);
         if (L.total <= budget) {
           x.occ_smem = ch.occ;
           x.trk_smem = ch.trk;
           x.stamp_bits = bits;
+          x.gstamp = ch.global ? r->stamps : nullptr;
           x.ring_bits = rb;
           x.cl = cl;
           x.warps = w;
@@ -593,6 +608,9 @@ extern "C" int cemc_run(const cemc_geometry *geo, const cemc_run_desc *r, void *
     if (e != cudaSuccess) return cuda_fail(e, "Monte Carlo kernel launch");
     done += n;
   }
+  r->kernel_used = form == cemc::kFormTable ? CEMC_KERNEL_TABLE
+                  : form == cemc::kFormGeneric ? CEMC_KERNEL_GENERIC
+                  : (a.tpw == 2 ? CEMC_KERNEL_SPIN_HALFWARP : CEMC_KERNEL_SPIN);
   if (form == cemc::kFormTable) {
     cudaError_t e = cemc::launch_recompute(g, r->n_chains, r->occ, r->eci, r->cf, r->energy, rscratch,
                                            static_cast<cudaStream_t>(stream));

@@ -16,6 +16,7 @@ struct RunArgs {
   int ring_bits;           // log2 of the draw / neighbour-row ring size
   int occ_smem, trk_smem;  // 1: the chain's occupation / swap tracker lives in shared memory
   int stamp_bits;          // log2 of the size of each of the two conflict-stamp tables
+  uint32_t *gstamp;        // exact stamp tables in global memory (2 << stamp_bits words per chain), or NULL
   uint64_t seed, n_trials;
   int8_t *occ;
   double *cf, *energy;
@@ -81,7 +82,7 @@ constexpr int kFormTable = 2;    // one lookup per cluster geometry; correlation
 
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
                                               int trk_smem, int stamp_bits, int n_cl, int n_masks, int ring_bits,
-                                              int form, int tpw) {
+                                              int form, int tpw, bool gstamp = false) {
   const bool spin = form == kFormSpin, table = form == kFormTable;
   McLayout L;
   size_t o = 0;
@@ -157,7 +158,7 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + L.warp_stride * (size_t)warps);
   L.stamp_bits = stamp_bits;
   L.stamp = o;
-  o = align16(o + 2 * 4 * ((size_t)1 << stamp_bits));
+  if (!gstamp) o = align16(o + 2 * 4 * ((size_t)1 << stamp_bits));
   L.occ = o;
   if (occ_smem) o = align16(o + (size_t)g.n_sites);
   L.trk = o;

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   const int CW = round_trials(CL, W, TPW);  // trials per round
   const int NB = n_bookers(CL, W, TPW);
   const McLayout L = mc_layout(g, W, MOVE, (int)sizeof(R), a.occ_smem, a.trk_smem, a.stamp_bits, SPIN ? sd.n_cl : 0,
-                               SPIN ? sd.n_masks : 0, a.ring_bits, FORM, TPW);
+                               SPIN ? sd.n_masks : 0, a.ring_bits, FORM, TPW, a.gstamp != nullptr);
   const uint32_t rmask = (1u << a.ring_bits) - 1u;
   const int rank = (CL == 2) ? (int)cluster_cta_rank() : 0;
   const unsigned peer = (unsigned)(rank ^ 1);
@@ -266,7 +266,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   uint64_t *nacc_slot = reinterpret_cast<uint64_t *>(misc + 36);  // [2] accept counts of this CTA's bookers
   Draw *draws = reinterpret_cast<Draw *>(smem + L.draws);
   int32_t *rows = reinterpret_cast<int32_t *>(smem + L.rows);
-  uint32_t *stamp = reinterpret_cast<uint32_t *>(smem + L.stamp);  // two tables of hmask + 1 entries
+  // two conflict-stamp tables of hmask + 1 entries: shared memory, or (large supercells,
+  // exact) this chain's region of a global buffer shared by both CTAs of a pair
+  const bool gst = a.gstamp != nullptr;
+  uint32_t *stamp = gst ? a.gstamp + (size_t)chain * 2 * (hmask + 1) : reinterpret_cast<uint32_t *>(smem + L.stamp);
   unsigned char *rec0 = smem + L.rec;
   // change rows of this CTA's trials: exact integers in the spin basis
   using DT = typename std::conditional<SPIN, int32_t, R>::type;
@@ -295,6 +298,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     loc = a.trk_smem ? trk + N : a.loc + (size_t)chain * N;
   }
 
+  // A chain with no trials in this launch (an empty serving slot) leaves its
+  // state untouched; both CTAs of a pair see the same count and leave together.
+  if (a.chain_trials && a.chain_trials[chain] <= a.chunk_offset) return;
+
   // ---- prologue: stage tables and the chain's state -------------------------
   for (int k = tid; k < n_eci; k += blockDim.x) {
     const int kind = g.eci_kind[k];
@@ -316,7 +323,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     uint2 *dst = reinterpret_cast<uint2 *>(terms_s);
     for (int i = tid; i < g.n_terms; i += blockDim.x) dst[i] = src[i];
   }
-  for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
+  if (!gst || rank == 0)
+    for (uint32_t i = tid; i < 2 * (hmask + 1); i += blockDim.x) stamp[i] = 0u;
   for (int i = tid; i < 2 * n_eci; i += blockDim.x) cfw[i] = acc_from<A>(0.0);
   if (!TAB)
     for (int i = tid; i < 2 * TPW * W * n_eci; i += blockDim.x)
@@ -896,22 +904,22 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
               if (nbra[q] >= 0) {
                 uint32_t *p = &tab[(uint32_t)nbra[q] & hmask];
                 atomicMax(p, mark);
-                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+                if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
               }
               if (SWAP && nbrb[q] >= 0) {
                 uint32_t *p = &tab[(uint32_t)nbrb[q] & hmask];
                 atomicMax(p, mark);
-                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+                if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
               }
             }
             if (lane == 0) {
               uint32_t *p = &tab[(uint32_t)sa & hmask];
               atomicMax(p, mark);
-              if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+              if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
               if (SWAP) {
                 p = &tab[(uint32_t)sb & hmask];
                 atomicMax(p, mark);
-                if (CL == 2) red_max_peer(peer_addr(p, peer), mark);
+                if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
               }
             }
           }

@@ -27,6 +27,7 @@ KERNEL_GENERIC = _lib.KERNEL_GENERIC
 KERNEL_SPIN = _lib.KERNEL_SPIN
 KERNEL_SPIN_HALFWARP = _lib.KERNEL_SPIN_HALFWARP
 KERNEL_TABLE = _lib.KERNEL_TABLE
+STAMP_GLOBAL_SITES = 16384  # larger supercells get exact conflict tables in device memory
 ACCUM_DOUBLES = _lib.ACCUM_DOUBLES
 # Field offsets (in doubles) of cemc_accum.
 A_EREF, A_SUM_E, A_SUM_E2, A_SUM_S, A_SUM_S2, A_SUM_SE, A_NSAMP, A_NACC = 0, 1, 2, 3, 7, 11, 15, 16
@@ -244,13 +245,30 @@ class ChainBatch:
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
-                         _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel())
+                         _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel(),
+                         _ptr(self._stamps()), self._stamp_buf.numel() if self._stamp_buf is not None else 0)
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
+        # the table form ends the call with a full recompute (cf and energy exact already)
+        self.last_kernel = int(d.kernel_used)
         if trace:
             return (tr[0].view(self.n_chains, n_trials, 2), tr[1].view(self.n_chains, n_trials),
                     tr[2].view(self.n_chains, n_trials))
         return None
+
+    def _stamps(self):
+        """Exact conflict tables in device memory for supercells whose shared-memory table would be hashed."""
+        if getattr(self, "_stamp_buf", None) is None:
+            self._stamp_buf = None
+            if self.geo.n_sites > STAMP_GLOBAL_SITES:
+                words = int(self.geo.L.cemc_stamp_words(self.geo.handle, self.n_chains))
+                self._stamp_buf = torch.empty(words, dtype=torch.int32, device=self.occ.device)
+        return self._stamp_buf
+
+    @property
+    def recomputed(self) -> bool:
+        """True when the last run already ended with a full recompute (table form)."""
+        return getattr(self, "last_kernel", 0) == KERNEL_TABLE
 
     def recompute(self):
         """Full FP64 correlation-function recompute of every chain; resets energy (``cemc_recompute``)."""

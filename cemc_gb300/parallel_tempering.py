@@ -87,7 +87,7 @@ class ParallelTempering:
         trials = max(1, int(round(sweeps_per_cycle * n_sites)))
         for _ in range(num_exchange_cycles):
             self.cb.run(trials, precision=self.precision, warps=self.warps)
-            if recompute:
+            if recompute and not self.cb.recomputed:
                 self.cb.recompute()
             E.pt_exchange(self.cb.energy, self.cb.kT, self.replica_of, self._direction(), self.seed,
                           self.exchange_round, self.n_accept, position_of=self.position_of)

@@ -5,11 +5,19 @@ serving layer the batched kernels make possible.  Jobs (supercell, cluster
 recipe, ECIs, ensemble, temperature, chemical potential, sweep budget) arrive
 at any time.  Jobs that share a geometry (supercell size and cluster set)
 share a device-resident slot batch; each batch advances all of its occupied
-slots by one quantum per tick in ONE launch of the fused kernel on its own
-CUDA stream, so batches of different geometries overlap on the device.  A
-job is admitted as soon as a slot of its batch is free and its state fits the
-HBM budget; it leaves when its budget is spent, and its slot is reused at the
-next tick.
+slots by one quantum in ONE launch of the fused kernel on its own CUDA
+stream, so batches of different geometries overlap on the device.  A job is
+admitted as soon as a slot of its batch is free and its state fits the HBM
+budget; it leaves when its budget is spent, and its slot is reused by the
+next launch of its batch.
+
+The loop is event driven: each batch keeps at most one launch in flight and
+is relaunched as soon as a CUDA event says its previous launch finished, so a
+batch of small supercells never waits for one of large supercells.  A batch's
+quantum (trials per slot per launch) is max(quantum_sweeps * N,
+quantum_trials): small supercells run many sweeps per launch (most of their
+jobs finish in one), large ones a few.  It depends on the geometry only, so a
+job's launches split its trials the same way alone or in any mix.
 
 A job's trials depend only on (seed, job key, trial index) and on its own
 state, and every quantum ends with the same FP64 recompute, so a job's result
@@ -91,6 +99,14 @@ class _Group:
         self.chain_trials = torch.zeros(capacity, dtype=torch.int64, device=geo.device)
         self.bytes_per_slot = n * (1 + (8 if move == E.MOVE_SWAP else 0)) + model.n_eci * 16 + 256
         self.launched = False
+        self.inflight = False
+        self.ev_done = torch.cuda.Event()
+        self.launch_trials = 0       # trials of the launch in flight
+        self.quantum = max(1, int(round(max(server.quantum * n, server.quantum_trials))))  # trials per slot
+        # Launch shape: small supercells on one SM per chain; large ones over a CTA pair (two
+        # SMs, rounds twice as wide) when the pair's shared memory fits (cemc_run decides).
+        self.warps, self.cluster = (server.warps, 1) if n < server.pair_sites else (server.warps, 0)
+        self.dirty = []  # slots loaded since the last launch: recomputed together before it
 
     def free_slot(self) -> int:
         for i, j in enumerate(self.jobs):
@@ -106,12 +122,17 @@ class MCServer:
     """Request loop: admit, tick, retire.
 
     :param hbm_budget_gb: device memory the server may hold in chain state and tables.
-    :param quantum_sweeps: sweeps per job per tick (one launch per batch per tick).
+    :param quantum_sweeps: at least this many sweeps per job per launch of its batch.
+    :param quantum_trials: at least this many trials per job per launch of its batch.
+    :param pair_sites: supercells of at least this many sites run a CTA pair per chain where the
+        library finds it fits; smaller ones one CTA.
+    :param capacity: slots per geometry batch (fewer for large supercells: about 2^20 sites per batch).
     :param capacity: slots per geometry batch.
     """
 
     def __init__(self, device="cuda", hbm_budget_gb: float = 120.0, quantum_sweeps: float = 10.0, capacity: int = 64,
-                 precision: int = E.PREC_F32, warps: int = 16, seed: int = 2026, kB: float = KB_EV):
+                 precision: int = E.PREC_F32, warps: int = 16, seed: int = 2026, kB: float = KB_EV,
+                 quantum_trials: int = 1 << 18, pair_sites: int = 8192):
         self.device = E.require_cuda(device)
         self.budget = hbm_budget_gb * 1e9
         self.used = 0.0
@@ -129,6 +150,8 @@ class MCServer:
         self._lock = threading.Lock()
         self.trials_done = 0
         self.t_start = None
+        self.quantum_trials = int(quantum_trials)
+        self.pair_sites = int(pair_sites)
 
     # -- submission ------------------------------------------------------------------
     def submit(self, job: Job) -> Job:
@@ -154,6 +177,17 @@ class MCServer:
             hit = (m, geo, eci)
             self.models[key] = hit
         return hit
+
+    def _capacity(self, m: CEModel) -> int:
+        return int(min(self.capacity, max(4, (1 << 20) // m.n_sites)))
+
+    def warm(self, jobs) -> float:
+        """Build the geometries the given jobs need ahead of time (a warm server); returns seconds."""
+        t0 = time.perf_counter()
+        for job in jobs:
+            self._model(job)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
 
     def _job_state(self, job: Job, m: CEModel, default_eci: dict):
         rng = np.random.default_rng(job.seed)
@@ -182,10 +216,10 @@ class MCServer:
             gkey = (job.L, job.recipe, move)
             grp = self.groups.get(gkey)
             if grp is None:
-                need = self.capacity * (m.n_sites * (9 if move == E.MOVE_SWAP else 1) + m.n_eci * 16 + 256)
+                need = self._capacity(m) * (m.n_sites * (9 if move == E.MOVE_SWAP else 1) + m.n_eci * 16 + 256)
                 if self.used + need > self.budget:
                     continue
-                grp = _Group(self, gkey, m, geo, move, self.capacity)
+                grp = _Group(self, gkey, m, geo, move, self._capacity(m))
                 self.groups[gkey] = grp
                 self.used += need
             slot = grp.free_slot()
@@ -217,42 +251,54 @@ class MCServer:
                 cb.loc[slot].copy_(torch.as_tensor(loc[0]))
                 cb.trk_start[slot].copy_(torch.as_tensor(start[0]))
                 cb.trk_count[slot].copy_(torch.as_tensor(count[0]))
-            self._recompute_slot(grp, slot)
-            cb.accum[slot].zero_()
-            cb.accum[slot, E.A_EREF] = cb.energy[slot]
+        grp.dirty.append(slot)
         grp.jobs[slot] = job
         grp.remaining[slot] = int(round(job.sweeps * m.n_sites))
 
-    def _recompute_slot(self, grp: _Group, slot: int):
-        cb = grp.cb
-        L = cb.geo.L
-        m = grp.model
-        el = 8
-        _lib.check(L.cemc_recompute(cb.geo.handle, 1, cb.occ.data_ptr() + slot * m.n_sites,
-                                    cb.eci.data_ptr() + slot * m.n_eci * el, cb.cf.data_ptr() + slot * m.n_eci * el,
-                                    cb.energy.data_ptr() + slot * el, cb.scratch.data_ptr(),
-                                    grp.stream.cuda_stream))
-
     # -- the loop ----------------------------------------------------------------------
+    def _launch(self, grp: _Group):
+        """One quantum of every occupied slot of a batch, asynchronous on its stream."""
+        if grp.dirty:
+            # newly loaded slots: one recompute of the batch (cf, energy), then fresh running sums
+            with torch.cuda.stream(grp.stream):
+                grp.cb.recompute()
+                idx = torch.as_tensor(grp.dirty, device=grp.cb.accum.device)
+                grp.cb.accum[idx] = 0.0
+                grp.cb.accum[idx, E.A_EREF] = grp.cb.energy[idx]
+            grp.dirty = []
+        per = np.minimum(grp.remaining, grp.quantum)
+        per[[j is None for j in grp.jobs]] = 0
+        n_max = int(per.max())
+        if n_max == 0:
+            return False
+        with torch.cuda.stream(grp.stream):
+            grp.chain_trials.copy_(torch.as_tensor(per), non_blocking=False)
+            grp.cb.run(n_max, precision=self.precision, warps=grp.warps, chain_trials=grp.chain_trials,
+                       cluster=grp.cluster)
+            if not grp.cb.recomputed:
+                grp.cb.recompute()
+            grp.ev_done.record(grp.stream)
+        grp.remaining -= per
+        grp.launch_trials = int(per.sum())
+        self.trials_done += grp.launch_trials
+        grp.inflight = True
+        return True
+
+    def _finish(self, grp: _Group):
+        """The batch's launch is done: hand out its finished jobs."""
+        grp.inflight = False
+        self._retire([grp])
+
     def _tick(self):
-        """Launch one quantum on every batch with active slots (each on its own stream)."""
+        """Relaunch every batch whose previous launch finished; returns the batches launched."""
         launched = []
         for grp in self.groups.values():
-            if grp.active() == 0:
-                continue
-            q = int(round(self.quantum * grp.model.n_sites))
-            per = np.minimum(grp.remaining, q)
-            per[[j is None for j in grp.jobs]] = 0
-            n_max = int(per.max())
-            if n_max == 0:
-                continue
-            with torch.cuda.stream(grp.stream):
-                grp.chain_trials.copy_(torch.as_tensor(per), non_blocking=False)
-                grp.cb.run(n_max, precision=self.precision, warps=self.warps, chain_trials=grp.chain_trials)
-                grp.cb.recompute()
-            grp.remaining -= per
-            self.trials_done += int(per.sum())
-            launched.append(grp)
+            if grp.inflight:
+                if not grp.ev_done.query():
+                    continue
+                self._finish(grp)
+            if grp.active() and self._launch(grp):
+                launched.append(grp)
         return launched
 
     def _retire(self, groups: List[_Group]):
@@ -283,12 +329,19 @@ class MCServer:
                 self.finished.append(job)
 
     def step(self) -> int:
-        """Admit, tick, retire once; returns the number of active jobs."""
+        """Admit, relaunch finished batches, hand out results once; returns the number of active jobs."""
         if self.t_start is None:
             self.t_start = time.perf_counter()
         self._admit()
         launched = self._tick()
-        self._retire(launched)
+        if not launched:
+            # nothing could start: wait for the first batch in flight instead of spinning
+            busy = [g for g in self.groups.values() if g.inflight]
+            if busy:
+                for _ in range(200):
+                    if any(g.ev_done.query() for g in busy):
+                        break
+                    time.sleep(0.0002)
         return sum(g.active() for g in self.groups.values())
 
     def run_until_idle(self, max_ticks: int = 10 ** 9):
@@ -301,9 +354,15 @@ class MCServer:
 
     def stats(self) -> dict:
         lat = np.array([j.latency for j in self.finished]) if self.finished else np.zeros(1)
+        wait = np.array([j.admitted - j.arrival for j in self.finished]) if self.finished else np.zeros(1)
+        run = np.array([j.done - j.admitted for j in self.finished]) if self.finished else np.zeros(1)
         wall = (time.perf_counter() - self.t_start) if self.t_start else 0.0
         return {"jobs": len(self.finished), "p50_latency_s": float(np.percentile(lat, 50)),
-                "p99_latency_s": float(np.percentile(lat, 99)), "trials": self.trials_done,
+                "p99_latency_s": float(np.percentile(lat, 99)),
+                "p50_admission_wait_s": float(np.percentile(wait, 50)),
+                "p99_admission_wait_s": float(np.percentile(wait, 99)),
+                "p50_run_s": float(np.percentile(run, 50)), "p99_run_s": float(np.percentile(run, 99)),
+                "trials": self.trials_done,
                 "trials_per_s": self.trials_done / wall if wall > 0 else 0.0, "wall_s": wall,
                 "hbm_used_gb": self.used / 1e9}
 

@@ -139,6 +139,12 @@ typedef struct {
   double *scratch;     /* table kernel: buffer for the final recompute (cemc_recompute_scratch_doubles()
                           doubles); NULL = the library's fixed array when it is large enough */
   uint64_t scratch_doubles;
+  uint32_t *stamps;    /* optional device buffer for exact conflict tables of large supercells, used when
+                          the shared-memory table would have to be hashed (hashing only costs speed):
+                          cemc_stamp_words() words; NULL = shared memory only */
+  uint64_t stamp_words;
+  int32_t kernel_used; /* output: the CEMC_KERNEL_* form cemc_run launched (CEMC_KERNEL_TABLE: the call
+                          already ended with a full recompute) */
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when
@@ -165,7 +171,12 @@ typedef struct {
  * functions and energy (replaces the Montecarlo._mc_step loop,
  * montecarlo.py:970-1038, over CEUpdater::calculate / undo_changes /
  * clear_history, ce_updater.cpp:313-555). */
-int cemc_run(const cemc_geometry *geo, const cemc_run_desc *run, void *stream);
+int cemc_run(const cemc_geometry *geo, cemc_run_desc *run, void *stream);
+
+/* Words of a cemc_run_desc.stamps buffer for n_chains chains of this geometry:
+ * two exact tables of 2^ceil(log2 N) entries per chain.  No reference counterpart
+ * (the reference evaluates one trial at a time and needs no conflict test). */
+size_t cemc_stamp_words(const cemc_geometry *geo, int32_t n_chains);
 
 /* Full correlation-function recompute over all sites of every chain, used for
  * validation and to reset FP64 drift; also rewrites energy = N * eci . cf.

@@ -310,3 +310,33 @@ def test_gpu_spin_kernel_rejects_ternary(E):
     from cemc_gb300._lib import CemcError
     with pytest.raises(CemcError):
         cb.run(10, kernel=E.KERNEL_SPIN)
+
+
+@pytest.mark.parametrize("move", [0, 1])
+def test_gpu_global_stamp_tables_match_oracle(move, E, oracle_mod, monkeypatch):
+    """55296 sites: the exact conflict table only fits in device memory; with it (exact) and
+    without it (hashed shared-memory table) the chain equals the oracle's."""
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(24, 4, 2, 1, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 3)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(5)
+    occ = rng.integers(0, 2, m.n_sites).astype(np.int8)
+    ev = m.eci_vector(eci)
+    kT = KB * 900.0
+    n = 20000
+    st = orc.new_chain_state(occ, ev, kT, move)
+    tr = orc.run(st, seed=31, chain_id=0, t_begin=0, n_trials=n, trace=True)
+    for global_tables in (True, False):
+        monkeypatch.setattr(E, "STAMP_GLOBAL_SITES", 0 if global_tables else 1 << 30)
+        cb = E.ChainBatch(geo, occ[None], ev, kT, move, seed=31)
+        _, acc, _ = cb.run(n, precision=E.PREC_F64, warps=30, trace=True, cluster=1)
+        _sync()
+        cb.check_status()
+        assert (cb._stamp_buf is not None) == global_tables
+        assert np.array_equal(acc.cpu().numpy()[0], tr.acc)
+        assert np.array_equal(cb.occ.cpu().numpy()[0], st.occ)
+        assert _cf_close(cb.cf.cpu().numpy()[0], st.cf)
