@@ -46,7 +46,8 @@ class GeometryDesc(C.Structure):
     _fields_ = [("n_sites", C.c_int32), ("n_cols", C.c_int32), ("n_sym", C.c_int32), ("n_bf", C.c_int32),
                 ("n_eci", C.c_int32), ("n_terms", C.c_int32),
                 ("table", _P), ("bf", _P), ("eci_kind", _P), ("eci_dec", _P), ("eci_weight", _P),
-                ("eci_full_weight", _P), ("term_eci", _P), ("term_ref", _P), ("term_size", _P), ("term_nb", _P)]
+                ("eci_full_weight", _P), ("term_eci", _P), ("term_ref", _P), ("term_size", _P), ("term_nb", _P),
+                ("movable", _P), ("n_movable", C.c_int32)]
 
 
 class RunDesc(C.Structure):

@@ -83,6 +83,21 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   if (one_idx + 1 + B >= (1 << cemc::kRefBits)) return fail(CEMC_ERR_LIMIT, "neighbour table too wide");
   for (size_t i = 0; i < (size_t)N * C; ++i)
     if (d->table[i] < 0 || d->table[i] >= N) return fail(CEMC_ERR_ARG, "table entry %zu out of range", i);
+  // Movable (non-background) sites: ascending, in range; every other site is background.
+  std::vector<int32_t> movable;
+  std::vector<int8_t> site_active(N, 1);
+  if (d->movable && d->n_movable < N) {
+    if (d->n_movable < 2) return fail(CEMC_ERR_ARG, "fewer than two movable sites");
+    movable.assign(d->movable, d->movable + d->n_movable);
+    std::fill(site_active.begin(), site_active.end(), 0);
+    for (int i = 0; i < d->n_movable; ++i) {
+      if (movable[i] < 0 || movable[i] >= N || (i > 0 && movable[i] <= movable[i - 1]))
+        return fail(CEMC_ERR_ARG, "movable sites must be ascending site indices");
+      site_active[movable[i]] = 1;
+    }
+  }
+  const int n_movable = movable.empty() ? N : (int)movable.size();
+  if (movable.empty()) movable.assign(1, 0);
   int singlet[CEMC_MAX_BF];
   for (int b = 0; b < CEMC_MAX_BF; ++b) singlet[b] = 0;
   for (int k = 0; k < K; ++k) {
@@ -346,6 +361,8 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {geo_list.data(), geo_list.size() * 4, 0},
       {pat_info.data(), pat_info.size() * 4, 0},
       {pat_terms.data(), pat_terms.size() * 4, 0},
+      {movable.data(), movable.size() * 4, 0},
+      {site_active.data(), site_active.size(), 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -399,6 +416,9 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.geo_list = reinterpret_cast<const uint4 *>(base + parts[21].off);
   g.pat_info = reinterpret_cast<const int4 *>(base + parts[22].off);
   g.pat_terms = reinterpret_cast<const int32_t *>(base + parts[23].off);
+  g.n_movable = n_movable;
+  g.movable = reinterpret_cast<const int32_t *>(base + parts[24].off);
+  g.site_active = n_movable == N ? nullptr : reinterpret_cast<const int8_t *>(base + parts[25].off);
   g.pm1_minus = -1;
   if (B == 1 && S == 2) {
     if (d->bf[0] == 1.0 && d->bf[1] == -1.0) g.pm1_minus = 1;

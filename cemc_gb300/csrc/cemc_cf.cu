@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kCfThreads) recompute_partial(DevGeo g, const 
   const int chain = blockIdx.y, bx = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int N = g.n_sites;
   const int i = bx * kCfThreads + tid;
-  const bool valid = i < N;
+  const bool valid = i < N && (!g.site_active || g.site_active[i]);  // background sites hold no clusters
   const int8_t *occ = occ_all + (size_t)chain * N;
   const int minus = g.pm1_minus;
   if (!PM1)

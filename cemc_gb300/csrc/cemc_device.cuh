@@ -53,6 +53,9 @@ struct DevGeo {
   const uint4 *geo_list;     // [n_geo] {columns c1 | c2 << 8 | c3 << 16 (absent: n_cols), F offset, S^m, 0}
   const int4 *pat_info;      // [n_pat] {m, F offset, first term, end term}
   const int32_t *pat_terms;  // k | d_ref << 8 | d1 << 12 | d2 << 16 | d3 << 20
+  int n_movable;             // sites that may change (n_sites when there is no background)
+  const int32_t *movable;    // [n_movable] ascending (used when n_movable < n_sites)
+  const int8_t *site_active; // [n_sites] 1 = movable; NULL when every site is
 };
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -448,7 +448,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         d.site = -1;
       } else {
         d.x0 = d.x1 = 0;
-        d.site = (int)cemc_below(w0.v[0], (uint32_t)N);
+        // the flipped site: uniform over the movable sites (all sites without a background)
+        d.site = g.n_movable == N ? (int)cemc_below(w0.v[0], (uint32_t)N)
+                                  : g.movable[cemc_below(w0.v[0], (uint32_t)g.n_movable)];
         const int32_t *src = g.table + (size_t)d.site * cpad;
         int32_t *dst = rows + (size_t)slot * cpad;
         for (int q = 0; q < cpad; q += 4) cp_async16(dst + q, src + q);

@@ -59,8 +59,6 @@ class Geometry:
         self.device = require_cuda(device)
         if not model.gpu_supported:
             raise NotImplementedError("the GPU path handles one translation-symmetry group with at most 4 decorations")
-        if len(model.background):
-            raise NotImplementedError("background sites are not supported on the GPU path yet")
         self.model = model
         self.L = _lib.load()
         m = model
@@ -75,12 +73,14 @@ class Geometry:
             "term_ref": np.ascontiguousarray(m.term_ref, dtype=np.int32),
             "term_size": np.ascontiguousarray(m.term_size, dtype=np.int32),
             "term_nb": np.ascontiguousarray(m.term_nb, dtype=np.int32),
+            "movable": np.ascontiguousarray(m.movable, dtype=np.int32),
         }
         h = self._host
         desc = _lib.GeometryDesc(m.n_sites, m.n_cols, m.n_sym, m.n_bf, m.n_eci, m.n_terms,
                                  *[h[n].ctypes.data for n in ("table", "bf", "eci_kind", "eci_dec", "eci_weight",
                                                               "eci_full_weight", "term_eci", "term_ref",
-                                                              "term_size", "term_nb")])
+                                                              "term_size", "term_nb")],
+                                 h["movable"].ctypes.data, int(len(m.movable)))
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.L.cemc_geometry_create(C.byref(desc), C.byref(handle)))
@@ -110,27 +110,33 @@ class Geometry:
         return int(self.L.cemc_recompute_scratch_doubles(self.handle, n_chains))
 
 
-def build_tracker(occ: np.ndarray, n_sym: int):
+def build_tracker(occ: np.ndarray, n_sym: int, background=None):
     """Per-species site lists of swap moves: sites of each species in site order.
 
     Same layout as ``SwapMoveIndexTracker.init_tracker``
     (cemc/mcmc/swap_move_index_tracker.py:22-33), flattened: species s owns
     trk[start[s] : start[s] + count[s]] and loc[site] is the site's slot.
+    Background sites are in no list (loc = -1); they sit after the last list.
     """
     occ = np.asarray(occ)
     n_chains, n = occ.shape
+    bg = np.zeros(n, dtype=bool)
+    if background is not None and len(background):
+        bg[np.asarray(background, dtype=np.int64)] = True
     trk = np.empty((n_chains, n), dtype=np.int32)
     loc = np.empty((n_chains, n), dtype=np.int32)
     start = np.zeros((n_chains, n_sym), dtype=np.int32)
     count = np.zeros((n_chains, n_sym), dtype=np.int32)
     for c in range(n_chains):
-        order = np.argsort(occ[c], kind="stable").astype(np.int32)
-        cnt = np.bincount(occ[c].astype(np.int64), minlength=n_sym).astype(np.int32)
+        key = np.where(bg, n_sym, occ[c].astype(np.int64))
+        order = np.argsort(key, kind="stable").astype(np.int32)
+        cnt = np.bincount(key, minlength=n_sym + 1).astype(np.int32)
         st = np.concatenate([[0], np.cumsum(cnt)[:-1]]).astype(np.int32)
         trk[c] = order
         loc[c, order] = np.arange(n, dtype=np.int32) - np.repeat(st, cnt)
-        start[c] = st
-        count[c] = cnt
+        loc[c, bg] = -1
+        start[c] = st[:n_sym]
+        count[c] = cnt[:n_sym]
     return trk, loc, start, count
 
 
@@ -169,7 +175,7 @@ class ChainBatch:
         self.chain_key = t(keys.astype(np.int32), torch.int32)
         self.trk = self.loc = self.trk_start = self.trk_count = None
         if self.move == MOVE_SWAP:
-            trk, loc, start, count = build_tracker(occ, m.n_sym)
+            trk, loc, start, count = build_tracker(occ, m.n_sym, m.background)
             present = (count > 0).sum(axis=1)
             if np.any(present < 2):
                 raise ValueError("swap moves need at least two species present in every chain")
@@ -214,7 +220,7 @@ class ChainBatch:
         """Per-species site lists from the current occupation (after external changes)."""
         m = self.geo.model
         occ = self.occ.cpu().numpy()
-        trk, loc, start, count = build_tracker(occ, m.n_sym)
+        trk, loc, start, count = build_tracker(occ, m.n_sym, m.background)
         if np.any((count > 0).sum(axis=1) < 2):
             raise ValueError("swap moves need at least two species present in every chain")
         dev = self.occ.device

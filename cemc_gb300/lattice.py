@@ -411,6 +411,54 @@ class Settings:
         return out
 
 
+class BackgroundSettings:
+    """Settings of a supercell with an inert second sublattice (background sites).
+
+    Rocksalt-like: the active sublattice is ``base`` (an FCC supercell of N sites,
+    indices 0..N-1, all clusters among them) and N background sites N..2N-1
+    hold ``background_symbol`` (e.g. O) that never moves and belongs to no
+    cluster (``ignore_background_atoms``; tests/test_sgc_mc.py:140-191 of the
+    reference runs that case with a ``FixedElement`` constraint).  Background
+    sites count in N (the singlet increment and the energy scale use the total,
+    ce_updater.cpp:366-371, 236-242) and have no translation-symmetry group.
+    Their rows of the translation matrix are empty dicts (the reference skips
+    background rows, ce_updater.cpp:925-927); the packed table maps them onto
+    themselves.
+    """
+
+    def __init__(self, base: Settings, background_symbol: str = "O"):
+        n = base.n_sites
+        self.base = base
+        self.cell = base.cell
+        self.cset = base.cset
+        self.unique_elements = list(base.unique_elements)
+        self.num_unique_elements = base.num_unique_elements
+        self.basis_functions = base.basis_functions
+        self.cluster_info = base.cluster_info
+        self.background_symbol = background_symbol
+        self.n_sites = 2 * n
+        self.index_by_trans_symm = [list(range(n))]
+        self.background_indices = list(range(n, 2 * n))
+        self.column_sites = base.column_sites
+        bg = np.arange(n, 2 * n, dtype=np.int32)
+        self.table = np.vstack([base.table, np.repeat(bg[:, None], base.table.shape[1], axis=1)]).astype(np.int32)
+        self._trans_list = None
+
+    @property
+    def trans_matrix(self):
+        if self._trans_list is None:
+            self._trans_list = list(self.base.trans_matrix) + [{} for _ in range(self.n_sites // 2)]
+        return self._trans_list
+
+    def symbols_with_background(self, active_symbols: Sequence[str]) -> List[str]:
+        """Atom symbols of the whole cell: the active sites' symbols, then the background symbol."""
+        return list(active_symbols) + [self.background_symbol] * (self.n_sites // 2)
+
+
+def with_background(settings: Settings, background_symbol: str = "O") -> BackgroundSettings:
+    return BackgroundSettings(settings, background_symbol)
+
+
 def fcc_settings(L: int, pair_shells: int, triplet_shells: int, quad_shells: int,
                  symbols: Sequence[str], a: float = 4.05) -> Settings:
     cset = fcc_cluster_set(pair_shells, triplet_shells, quad_shells, len(symbols))

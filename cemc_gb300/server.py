@@ -246,7 +246,7 @@ class MCServer:
             cb.chain_key[slot] = (job.seed * 2654435761 + 97) & 0x7FFFFFFF
             if grp.move == E.MOVE_SWAP:
                 from .engine import build_tracker
-                trk, loc, start, count = build_tracker(occ[None], m.n_sym)
+                trk, loc, start, count = build_tracker(occ[None], m.n_sym, m.background)
                 cb.trk[slot].copy_(torch.as_tensor(trk[0]))
                 cb.loc[slot].copy_(torch.as_tensor(loc[0]))
                 cb.trk_start[slot].copy_(torch.as_tensor(start[0]))

@@ -69,6 +69,7 @@ class CEModel:
         self.group_count = np.array([int((site_group == gi).sum()) for gi in range(self.n_groups)], dtype=np.int32)
         self.movable = np.nonzero(site_group >= 0)[0].astype(np.int32)
         self.background = np.array(sorted(background), dtype=np.int32)
+        self.background_symbol = getattr(settings, "background_symbol", None)
 
         # Basis functions bf[dec, id] (basis_function.cpp:5-19).
         bf = np.zeros((self.n_bf, self.n_sym))
@@ -122,6 +123,8 @@ class CEModel:
             self.members[r, :len(sub)] = [col_of[x] for x in sub]
             self.order[r, :len(order)] = order
         self.table = self._read_table(settings, cols)
+        if len(self.background):  # background rows are never read; they point at the site itself
+            self.table[self.background] = self.background[:, None]
 
         # ECIs in sorted-name order.
         names = sorted(eci_names)
@@ -177,7 +180,8 @@ class CEModel:
             out = np.zeros((len(tm), len(cols)), dtype=np.int32)
             for i, row in enumerate(tm):
                 if not row:
-                    continue  # background rows are never read
+                    out[i] = i  # background rows are never read; they point at the site itself
+                    continue
                 out[i] = [int(row[c]) for c in cols]
             return out
         tm = np.asarray(tm, dtype=np.int32)
@@ -229,8 +233,15 @@ class CEModel:
         return np.array([float(eci.get(n, 0.0)) for n in self.eci_names])
 
     def occupation(self, symbols: Sequence[str]) -> np.ndarray:
+        """Species ids of atom symbols; background sites get the placeholder id 0."""
         lut = {s: i for i, s in enumerate(self.symbols)}
-        return np.array([lut[s] for s in symbols], dtype=np.int8)
+        bg = set(self.background.tolist())
+        return np.array([0 if i in bg else lut[s] for i, s in enumerate(symbols)], dtype=np.int8)
 
     def symbols_of(self, occ: np.ndarray) -> List[str]:
-        return [self.symbols[int(i)] for i in occ]
+        """Atom symbols of species ids; background sites read the settings' background symbol."""
+        out = [self.symbols[int(i)] for i in occ]
+        if self.background_symbol is not None:
+            for i in self.background.tolist():
+                out[i] = self.background_symbol
+        return out

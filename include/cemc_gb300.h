@@ -76,6 +76,12 @@ typedef struct {
   const int32_t *term_ref;   /* [n_terms] */
   const int32_t *term_size;  /* [n_terms] */
   const int32_t *term_nb;    /* [n_terms * 3] */
+  /* Sites that may change (not background, ce_updater.cpp:1015-1026), ascending; single-site
+   * flips draw their site from this list and swap trackers hold only these sites; background
+   * sites keep species id 0 in the occupations, belong to no cluster and are skipped by the
+   * full recompute.  NULL (or n_movable == n_sites) = every site. */
+  const int32_t *movable;
+  int32_t n_movable;
 } cemc_geometry_desc;
 
 typedef struct cemc_geometry cemc_geometry;

@@ -28,11 +28,14 @@ def load_golden(name):
 
 def golden_model(g):
     """Rebuild the settings/model of a golden case and check it is the generated one."""
-    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis, with_background
     from cemc_gb300.tables import CEModel
     ps, ts, qs = (int(x) for x in g["shells"])
     syms = [str(s) for s in g["species"]]
     s = fcc_settings(int(g["L"]), ps, ts, qs, syms)
+    bg = str(g["background"]) if "background" in g else ""
+    if bg:
+        s = with_background(s, bg)
     eci = seeded_ecis(s.cset, 0)
     m = CEModel(s, list(eci))
     return s, m, eci

@@ -35,18 +35,22 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from cemc_gb300.lattice import fcc_settings, seeded_ecis  # noqa: E402
+from cemc_gb300.lattice import fcc_settings, seeded_ecis, with_background  # noqa: E402
 from cemc_gb300.tables import CEModel  # noqa: E402
 
 KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
 
-# name, L, pair shells, triplet shells, quad shells, species, move (0 flip, 1 swap), T, trials, seed
+# name, L, pair shells, triplet shells, quad shells, species, move (0 flip, 1 swap), T, trials, seed,
+# background symbol (None: every site active; else an inert second sublattice of that species,
+# rocksalt-like, as in the reference's tests/test_sgc_mc.py:140-191)
 CASES = [
-    ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11),
-    ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12),
-    ("binary_swap_cold", 4, 4, 2, 1, ["Al", "Mg"], 1, 150.0, 3000, 13),
-    ("ternary_flip", 4, 5, 3, 1, ["Al", "Mg", "Si"], 0, 800.0, 1500, 14),
-    ("ternary_swap", 4, 5, 3, 1, ["Al", "Mg", "Si"], 1, 800.0, 1500, 15),
+    ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11, None),
+    ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12, None),
+    ("binary_swap_cold", 4, 4, 2, 1, ["Al", "Mg"], 1, 150.0, 3000, 13, None),
+    ("ternary_flip", 4, 5, 3, 1, ["Al", "Mg", "Si"], 0, 800.0, 1500, 14, None),
+    ("ternary_swap", 4, 5, 3, 1, ["Al", "Mg", "Si"], 1, 800.0, 1500, 15, None),
+    ("rocksalt_flip", 4, 4, 2, 1, ["Li", "V"], 0, 800.0, 3000, 16, "O"),
+    ("rocksalt_swap", 4, 4, 2, 1, ["Li", "V"], 1, 800.0, 3000, 17, "O"),
 ]
 
 
@@ -58,21 +62,30 @@ def model_hash(m: CEModel) -> str:
     return h.hexdigest()
 
 
-def build_case(name, L, ps, ts, qs, syms, move, T, n, seed):
+def build_case(name, L, ps, ts, qs, syms, move, T, n, seed, background):
     import oracle as O
     s = fcc_settings(L, ps, ts, qs, syms)
+    if background:
+        s = with_background(s, background)
     eci = seeded_ecis(s.cset, 0)
     m = CEModel(s, list(eci))
     orc = O.Oracle(m)
     rng = np.random.default_rng(seed)
     occ0 = rng.integers(0, len(syms), m.n_sites).astype(np.int8)
+    occ0[m.background] = 0  # background sites keep a placeholder id; the reference sees the background symbol
+
+    def ref_symbols(occ):
+        out = m.symbols_of(occ)
+        for i in m.background:
+            out[int(i)] = background
+        return out
     ev = m.eci_vector(eci)
     kT = KB * T
     st = orc.new_chain_state(occ0, ev, kT, move)
     cf0 = st.cf.copy()
     tr = orc.run(st, seed=seed, chain_id=0, t_begin=0, n_trials=n, trace=True)
 
-    upd, _ = O.make_reference_updater(s, m.symbols_of(occ0), dict(zip(m.eci_names, cf0)), eci)
+    upd, _ = O.make_reference_updater(s, ref_symbols(occ0), dict(zip(m.eci_names, cf0)), eci)
     occ = occ0.copy()
     cur = upd.get_energy()
     acc = np.zeros(n, dtype=np.int8)
@@ -99,10 +112,10 @@ def build_case(name, L, ps, ts, qs, syms, move, T, n, seed):
     cf_final = np.array([ref_cf[k] for k in m.eci_names])
 
     # Known answers of explicit single-site updates (CEUpdater::update_cf).
-    upd2, _ = O.make_reference_updater(s, m.symbols_of(occ0), dict(zip(m.eci_names, cf0)), eci)
+    upd2, _ = O.make_reference_updater(s, ref_symbols(occ0), dict(zip(m.eci_names, cf0)), eci)
     occ_u = occ0.copy()
     n_upd = 12
-    upd_sites = rng.choice(m.n_sites, n_upd, replace=False).astype(np.int32)
+    upd_sites = rng.choice(m.movable, n_upd, replace=False).astype(np.int32)
     upd_new = np.zeros(n_upd, dtype=np.int8)
     upd_cf = np.zeros((n_upd, m.n_eci))
     upd_e = np.zeros(n_upd)
@@ -117,6 +130,7 @@ def build_case(name, L, ps, ts, qs, syms, move, T, n, seed):
 
     return dict(
         L=L, shells=np.array([ps, ts, qs]), species=np.array(syms), move=move, T=T, kT=kT, seed=seed,
+        background=np.array(background or ""),
         n_trials=n, model_hash=model_hash(m), eci=ev, eci_names=np.array(m.eci_names),
         occ0=occ0, cf0=cf0, sites=tr.site.reshape(n, 2), u=tr.u, ref_acc=acc, ref_de=de,
         occ_final=occ, cf_final=cf_final, energy_final=cur,
@@ -127,7 +141,10 @@ def build_case(name, L, ps, ts, qs, syms, move, T, n, seed):
 def main():
     import contextlib
     out_dir = HERE
+    only = set(sys.argv[1:])  # case names to (re)generate; default all
     for case in CASES:
+        if only and case[0] not in only:
+            continue
         # the reference's init logs to the C++ streams; silence them at the fd level
         with open(os.devnull, "w") as devnull, contextlib.ExitStack():
             saved = os.dup(1), os.dup(2)
