@@ -488,9 +488,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
     return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs single-site flips with at most 16 cluster ECIs");
-  if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && r->cluster == 2)
-    return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs one CTA per chain");
   // two trials per warp: asked for, or chosen when eligible and no CTA pair was asked for
+  // (a CTA pair takes the half-warp form only when that form is asked for explicitly)
   const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
                                                                 r->cluster != 2)) ? 2 : 1;
   int warps = r->warps > 0 ? r->warps : 16;
@@ -583,7 +582,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   bool found = false;
   for (size_t fi = 0; fi < forms.size() && !found; ++fi) {
     form = forms[fi];
-    if (tpw == 1 && (r->cluster == 2 || (r->cluster == 0 && 2 * r->n_chains <= geo->n_sms))) {
+    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && 2 * r->n_chains <= geo->n_sms)) {
       cemc::RunArgs x = a;
       cemc::McLayout L2{};
       if (fit(2, L2, x)) {

@@ -47,7 +47,8 @@ __host__ __device__ inline int n_bookers(int cl, int warps, int tpw) {
 }
 // Evaluating warps per CTA that fit next to the helpers in 1024 threads.
 __host__ __device__ inline int max_eval_warps(int cl, int tpw) {
-  return (cl == 1 && tpw == 2) ? 29 : kMaxEval;
+  if (tpw == 2) return cl == 1 ? 29 : kRoundSlots / 4;  // a pair of half-warp CTAs: 4 trials per warp index
+  return kMaxEval;
 }
 // Ring size (log2): more than kPrefetchRounds rounds of trials.
 __host__ __device__ inline int ring_bits_for(int cw) { return kPrefetchRounds * cw < 128 ? 7 : 8; }

@@ -542,8 +542,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   // slots [own_lo, own_hi) (change rows dbuf[slot - own_lo] in a pair, dbuf[slot]
   // otherwise), summed by the booker: lane takes ECIs lane, lane + 32, ... in
   // registers; exact 64-bit integers for the spin basis (integer changes).
-  const int own_lo = (CL == 2) ? rank * W : 32 * bq;
-  const int own_hi = (CL == 2) ? own_lo + W : own_lo + 32;
+  const int own_lo = (CL == 2) ? rank * W * TPW : 32 * bq;
+  const int own_hi = (CL == 2) ? own_lo + W * TPW : own_lo + 32;
   A *cfb = cfw + (size_t)(CL == 1 ? bq : 0) * n_eci;
   using CFA = typename std::conditional<SPIN, long long, A>::type;
   CFA cfr[4];
@@ -684,9 +684,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       DT *Dw = dbuf + (size_t)warp * n_eci;
       if (TPW == 2) {
         // ---- phase A, two flips per warp: half h = lane / 16 evaluates trial slot 2 warp + h ----
-        if (active && t0 + (uint64_t)(2 * warp) < t_end) {
+        if (active && t0 + (uint64_t)(rank * 2 * W + 2 * warp) < t_end) {
           const int h = lane >> 4, hl = lane & 15;
-          const int gh = 2 * warp + h;
+          const int gh = rank * 2 * W + 2 * warp + h;  // trial slot in the round (pairs: CTA 1 after CTA 0)
           const uint64_t t = t0 + (uint64_t)gh;
           const bool has = t < t_end;  // the second half of the last warp may have no trial
           const uint32_t slot = (uint32_t)t & rmask;
@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           const int32_t *row = rows + (size_t)slot * cpad;
           int nbr[4];
           uint32_t wl = 0, wh = 0;
-  #pragma unroll
+#pragma unroll
           for (int j = 0; j < 4; ++j) {
             const int c = hl + 16 * j;
             uint32_t bit = 0;
@@ -735,14 +735,14 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             if (hl == k) my_odd = (int)((tot >> (16 * h)) & 0xFFFFu);
           }
           const int delta = occ_a_bit ? 2 : -2;
-          DT *Dh = dbuf + (size_t)gh * n_eci;
+          DT *Dh = dbuf + (size_t)(2 * warp + h) * n_eci;  // this CTA's change row of the trial
           int P = 0;
           if (hl < sd.n_cl) {
             P = sp_e.n_pairs - 2 * (__popc(wl & sp_e.pair_lo) + __popc(wh & sp_e.pair_hi)) + sp_e.n_multi - 2 * my_odd;
             if (has) Dh[sp_e.eci] = delta * P;
           }
           R sum = sp_coef * (R)P;
-  #pragma unroll
+#pragma unroll
           for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
           if (sd.singlet_eci >= 0) {
             if (hl == 0 && has) Dh[sd.singlet_eci] = delta;
@@ -752,19 +752,27 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           int acc = 0;
           if (hl == 0 && has) {
             acc = metropolis<R>(de, ua, ub, kT, inv_kT);
-            r_sa[gh] = sa;
-            r_sb[gh] = na;
-            r_acc[gh] = (int8_t)acc;
-            r_de[gh] = de;
-            r_ds[gh] = (R)delta;  // the singlet change (one decoration)
+            put(&r_sa[gh], (int32_t)sa);
+            put(&r_sb[gh], (int32_t)na);
+            put(&r_acc[gh], (int8_t)acc);
+            put(&r_de[gh], de);
+            put(&r_ds[gh], (R)delta);  // the singlet change (one decoration)
           }
           acc = __shfl_sync(kFull, acc, 16 * h);
           if (acc) {
             const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
-  #pragma unroll
+#pragma unroll
             for (int j = 0; j < 4; ++j)
-              if (nbr[j] >= 0) atomicMax(&tab[(uint32_t)nbr[j] & hmask], mark);
-            if (hl == 0) atomicMax(&tab[(uint32_t)sa & hmask], mark);
+              if (nbr[j] >= 0) {
+                uint32_t *p = &tab[(uint32_t)nbr[j] & hmask];
+                atomicMax(p, mark);
+                if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
+              }
+            if (hl == 0) {
+              uint32_t *p = &tab[(uint32_t)sa & hmask];
+              atomicMax(p, mark);
+              if (CL == 2 && !gst) red_max_peer(peer_addr(p, peer), mark);
+            }
           }
         }
       } else {
@@ -901,7 +909,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           acc = __shfl_sync(kFull, acc, 0);
           if (acc) {
             const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
-  #pragma unroll
+#pragma unroll
             for (int q = 0; q < 4; ++q) {
               if (nbra[q] >= 0) {
                 uint32_t *p = &tab[(uint32_t)nbra[q] & hmask];
@@ -1128,7 +1136,9 @@ static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t 
     return launch_f<R, CEMC_MOVE_SWAP, kFormGeneric>(g, a, smem, st, none);
   }
   if (form == kFormSpin) {
-    if (a.tpw == 2) return launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 1, 2>(g, a, smem, st, *spin);
+    if (a.tpw == 2)
+      return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 2, 2>(g, a, smem, st, *spin)
+                       : launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 1, 2>(g, a, smem, st, *spin);
     return launch_f<R, CEMC_MOVE_FLIP, kFormSpin>(g, a, smem, st, *spin);
   }
   if (form == kFormTable) return launch_f<R, CEMC_MOVE_FLIP, kFormTable>(g, a, smem, st, none);
@@ -1138,7 +1148,7 @@ static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t 
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       int form, const SpinDev *spin) {
   // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
-  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP || a.cl != 1)) return cudaErrorInvalidValue;
+  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP)) return cudaErrorInvalidValue;
   if (form == kFormSpin && !spin) return cudaErrorInvalidValue;
   return precision == CEMC_PREC_F32 ? launch_r<float>(g, a, move, smem, st, form, spin)
                                     : launch_r<double>(g, a, move, smem, st, form, spin);

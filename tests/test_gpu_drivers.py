@@ -228,3 +228,67 @@ def test_fp32_drift_and_recompute_at_benchmark_size(torch_cuda):
     # singlet = mean spin (a size-independent identity)
     spins = np.where(cb.occ.cpu().numpy() == 0, 1.0, -1.0).mean(axis=1)
     assert np.allclose(cf_full[:, m.eci_names.index("c1_0")], spins, atol=1e-14)
+
+
+def test_multi_geometry_graph_equals_separate_batches(torch_cuda):
+    """One CUDA graph over chains of three supercell sizes (and both move types) steps each
+    group exactly as its own batch runner does."""
+    from cemc_gb300 import engine as E
+    from cemc_gb300.batch import BatchRunner, MultiBatchRunner
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    specs = [(4, (4, 2, 1), ("Al", "Mg"), E.MOVE_FLIP), (5, (5, 3, 1), ("Al", "Mg", "Si"), E.MOVE_SWAP),
+             (6, (4, 2, 1), ("Al", "Mg"), E.MOVE_SWAP)]
+
+    def runners():
+        out = []
+        for L, sh, syms, move in specs:
+            s = fcc_settings(L, *sh, list(syms))
+            eci = seeded_ecis(s.cset, L)
+            m = CEModel(s, list(eci))
+            geo = E.Geometry(m)
+            rng = np.random.default_rng(L)
+            occ = rng.integers(0, len(syms), (3, m.n_sites)).astype(np.int8)
+            out.append(BatchRunner(geo, occ, m.eci_vector(eci), [500.0, 900.0, 1300.0], move, seed=3 + L,
+                                   precision=E.PREC_F32, warps=8, sweeps_per_step=2.0, graph=True))
+        return out
+
+    alone = runners()
+    for r in alone:
+        r.step(3)
+        r.synchronize()
+    multi = MultiBatchRunner(runners())
+    multi.step(3)
+    multi.synchronize()
+    for a, b in zip(alone, multi.runners):
+        a.cb.check_status()
+        b.cb.check_status()
+        assert np.array_equal(a.cb.occ.cpu().numpy(), b.cb.occ.cpu().numpy())
+        assert np.array_equal(a.cb.cf.cpu().numpy(), b.cb.cf.cpu().numpy())
+        assert np.array_equal(a.cb.accum_host(), b.cb.accum_host())
+
+
+def test_table_form_leaves_exact_correlation_functions(torch_cuda, oracle_mod):
+    """The table form ends cemc_run with the full recompute: CFs and energy equal the oracle's
+    full recompute of the final occupation, and callers see kernel_used = table."""
+    from cemc_gb300 import engine as E
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(5, 5, 3, 1, ["Al", "Mg", "Si"])
+    eci = seeded_ecis(s.cset, 2)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(4)
+    occ = rng.integers(0, 3, (4, m.n_sites)).astype(np.int8)
+    for move in (E.MOVE_FLIP, E.MOVE_SWAP):
+        cb = E.ChainBatch(geo, occ, m.eci_vector(eci), KB * 700.0, move, seed=9)
+        cb.run(4 * m.n_sites, precision=E.PREC_F32, warps=12, kernel=E.KERNEL_TABLE)
+        torch_cuda.cuda.synchronize()
+        assert cb.last_kernel == E.KERNEL_TABLE and cb.recomputed
+        for c in range(4):
+            o = cb.occ.cpu().numpy()[c]
+            full = orc.full_cf(o)
+            assert np.allclose(cb.cf.cpu().numpy()[c], full, rtol=1e-12, atol=1e-15)
+            assert abs(cb.energy.cpu().numpy()[c] - orc.energy(m.eci_vector(eci), full)) < 1e-9 * abs(
+                orc.energy(m.eci_vector(eci), full))

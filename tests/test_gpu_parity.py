@@ -57,8 +57,8 @@ def _kernel_ok(m, kernel, E, move=0, cluster=0):
     if kernel in (E.KERNEL_SPIN, E.KERNEL_SPIN_HALFWARP) and not (
             m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0]):
         pytest.skip("spin-basis kernel needs a binary +1/-1 basis")
-    if kernel == E.KERNEL_SPIN_HALFWARP and (move != 0 or cluster == 2):
-        pytest.skip("the half-warp spin kernel runs flips on one CTA per chain")
+    if kernel == E.KERNEL_SPIN_HALFWARP and move != 0:
+        pytest.skip("the half-warp spin kernel runs flips")
 
 
 KERNELS = [1, 2, 3, 4]  # generic, spin, spin half-warp, table
@@ -228,8 +228,8 @@ def test_gpu_launch_splitting_is_invisible(kernel, E):
     b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=4)
     a.run(3000, precision=0, warps=16, kernel=kernel, cluster=1)
     for i in range(3):
-        if i == 1:  # the middle piece on a CTA pair (the half-warp form runs one CTA: use the warp-per-trial form)
-            b.run(1000, precision=0, warps=7, kernel=E.KERNEL_SPIN if half else kernel, cluster=2)
+        if i == 1:  # the middle piece on a CTA pair
+            b.run(1000, precision=0, warps=7, kernel=kernel, cluster=2)
         else:
             b.run(1000, precision=0, warps=7, kernel=kernel, cluster=1)
     _sync()
