@@ -375,6 +375,55 @@ def run_pt(args):
     return 0
 
 
+def run_canonical1(args):
+    """One canonical swap chain in FP64: binary FCC 8x8x8 (2048 sites), 50/50 random init (seed 0),
+    T = 800 K, the headline cluster set and ECI recipe; 2048 x 1000 swaps per step.
+
+    The GPU form of the reference's plain single-chain run (CPU-runnable size).  Also times the
+    CPU restatement of the reference updater and Metropolis loop on one host thread for the same
+    chain (a bounded sample)."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from cemc_gb300 import engine as E
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(8, *SHELLS, SPECIES)
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    geo = E.Geometry(m, dev)
+    rng = np.random.default_rng(0)
+    occ = np.zeros(m.n_sites, dtype=np.int8)
+    occ[rng.permutation(m.n_sites)[: m.n_sites // 2]] = 1
+    ev = m.eci_vector(eci)
+    cb = E.ChainBatch(geo, occ[None], ev, KB * 800.0, E.MOVE_SWAP, seed=0)
+    n = m.n_sites * 1000
+    stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
+    t, clocks = _timed_steps(lambda: cb.run(n, precision=E.PREC_F64, warps=args.warps or 16), stream, args.steps,
+                             args.warmup, local)
+    cb.check_status()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        orc = O.Oracle(m)
+        st = orc.new_chain_state(occ, ev, KB * 800.0, O.MOVE_SWAP)
+        n_cpu = 200000
+        t0 = time.perf_counter()
+        orc.run(st, seed=0, chain_id=0, t_begin=0, n_trials=n_cpu)
+        cpu = {"value": n_cpu / (time.perf_counter() - t0), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "%d swaps of the same chain on one host thread" % n_cpu}
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "workload": "canonical_single_chain", "value": n * args.steps / t,
+                          "unit": UNIT, "ms_per_step": t * 1e3 / args.steps, "steps": args.steps,
+                          "warmup": args.warmup, "dtype": "f64", "clocks": clocks, "cpu_baseline": cpu,
+                          "accept_rate": float(cb.accum_host()[0, E.A_NACC] / max(cb.accum_host()[0, E.A_NSAMP], 1)),
+                          "config": {"workload": "canonical_swap_fcc_binary_8x8x8_1chain", "n_sites": m.n_sites,
+                                     "trials_per_step": n, "T": 800.0, "precision": "fp64"}}))
+    return 0
+
+
 def run_recompute(args):
     """Full correlation-function recompute (cemc_recompute) alone, on the ladder geometry.
 
@@ -636,10 +685,11 @@ def main(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)
     p.add_argument("--no-correctness", action="store_true")
-    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served", "recompute", "ternary", "pt"],
+    p.add_argument("--workload", default="sgc64", choices=["sgc64", "served", "recompute", "ternary", "pt", "canonical1"],
                    help="sgc64: the headline 64-chain batch; served: the Poisson job stream; "
                         "recompute: the full correlation-function recompute alone; ternary: 256 ternary "
-                        "chains of uneven size in one graph launch; pt: the 48-replica tempering ladder")
+                        "chains of uneven size in one graph launch; pt: the 48-replica tempering ladder; "
+                        "canonical1: one FP64 canonical chain of 2048 sites")
     p.add_argument("--ternary-chains", type=int, default=256)
     p.add_argument("--recompute-cell", type=int, default=32)
     p.add_argument("--recompute-chains", type=int, default=48)
@@ -661,6 +711,8 @@ def main(argv=None):
         return run_ternary(args)
     if args.workload == "pt":
         return run_pt(args)
+    if args.workload == "canonical1":
+        return run_canonical1(args)
     return run_gpu(args)
 
 
