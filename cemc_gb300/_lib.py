@@ -29,6 +29,7 @@ KERNEL_SPIN = 2
 KERNEL_SPIN_HALFWARP = 3
 KERNEL_TABLE = 4
 MAX_BF = 4
+MAX_GROUPS = 8
 
 _P = C.c_void_p
 
@@ -47,7 +48,8 @@ class GeometryDesc(C.Structure):
                 ("n_eci", C.c_int32), ("n_terms", C.c_int32),
                 ("table", _P), ("bf", _P), ("eci_kind", _P), ("eci_dec", _P), ("eci_weight", _P),
                 ("eci_full_weight", _P), ("term_eci", _P), ("term_ref", _P), ("term_size", _P), ("term_nb", _P),
-                ("movable", _P), ("n_movable", C.c_int32)]
+                ("movable", _P), ("n_movable", C.c_int32),
+                ("n_groups", C.c_int32), ("site_group", _P), ("group_terms", _P), ("group_scale", _P)]
 
 
 class RunDesc(C.Structure):

@@ -34,7 +34,7 @@ def _key(geo, move, precision, n_chains) -> str:
     m = geo.model
     # chains only matter up to one per SM
     sms = torch.cuda.get_device_properties(geo.device).multi_processor_count
-    return "|".join(map(str, ("shape", name, m.n_sites, m.n_cols, m.n_terms, m.n_eci, move, precision,
+    return "|".join(map(str, ("shape", name, m.n_sites, m.gpu_n_cols, m.n_groups, m.n_terms, m.n_eci, move, precision,
                               min(int(n_chains), sms))))
 
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <map>
 #include <mutex>
@@ -107,10 +108,37 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       singlet[d->eci_dec[k]] = k;
     }
   }
+  // Translation-symmetry groups: each owns a contiguous, ECI-sorted range of
+  // terms; a one-group geometry is group 0 with every term.
+  const int G = d->n_groups > 1 ? d->n_groups : 1;
+  if (G > CEMC_MAX_GROUPS) return fail(CEMC_ERR_LIMIT, "%d translation groups exceed the limit %d", G, CEMC_MAX_GROUPS);
+  std::vector<int32_t> gterm(G + 1, 0);
+  std::vector<double> gscale(G, 1.0);
+  std::vector<int8_t> sgroup(N, 0);
+  gterm[G] = T;
+  if (G > 1) {
+    if (!d->site_group || !d->group_terms || !d->group_scale) return fail(CEMC_ERR_ARG, "null group table");
+    for (int q = 0; q <= G; ++q) gterm[q] = d->group_terms[q];
+    if (gterm[0] != 0 || gterm[G] != T) return fail(CEMC_ERR_ARG, "group term ranges must cover the terms");
+    for (int q = 0; q < G; ++q) {
+      if (gterm[q + 1] < gterm[q]) return fail(CEMC_ERR_ARG, "group term ranges must ascend");
+      gscale[q] = d->group_scale[q];
+      if (!(gscale[q] > 0.0) || !std::isfinite(gscale[q])) return fail(CEMC_ERR_ARG, "bad group scale");
+    }
+    for (int i = 0; i < N; ++i) {
+      if (!site_active[i]) continue;
+      const int q = d->site_group[i];
+      if (q < 0 || q >= G) return fail(CEMC_ERR_ARG, "site %d has no translation group", i);
+      sgroup[i] = (int8_t)q;
+    }
+  }
+  bool equal_groups = true;
+  for (int q = 0; q < G; ++q) equal_groups = equal_groups && gscale[q] == 1.0;
   for (int t = 0; t < T; ++t) {
     const int k = d->term_eci[t];
+    const bool group_start = std::find(gterm.begin(), gterm.end(), t) != gterm.end();
     if (k < 0 || k >= K || d->eci_kind[k] != 2) return fail(CEMC_ERR_ARG, "term %d has a bad ECI", t);
-    if (t > 0 && k < d->term_eci[t - 1]) return fail(CEMC_ERR_ARG, "terms are not sorted by ECI");
+    if (t > 0 && !group_start && k < d->term_eci[t - 1]) return fail(CEMC_ERR_ARG, "terms are not sorted by ECI");
     if (d->term_size[t] < 2 || d->term_size[t] > 4) return fail(CEMC_ERR_ARG, "term %d has a bad size", t);
     if (d->term_ref[t] < 0 || d->term_ref[t] >= B) return fail(CEMC_ERR_ARG, "term %d has a bad decoration", t);
     for (int j = 0; j < d->term_size[t] - 1; ++j)
@@ -118,41 +146,45 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
         return fail(CEMC_ERR_ARG, "term %d has a bad member", t);
   }
 
-  // Lane chunks.
-  std::vector<int32_t> lane_term(33), first(32, 0), eci_lane(2 * (size_t)K);
-  for (int l = 0; l <= 32; ++l) lane_term[l] = (int32_t)(((long long)l * T) / 32);
+  // Lane chunks, per group: [G][33] bounds, [G][32] first ECI, [G][2K] lane range per ECI.
+  std::vector<int32_t> lane_term(33 * (size_t)G), first(32 * (size_t)G, 0), eci_lane(2 * (size_t)K * G);
   int n_slots = 1;
-  for (int k = 0; k < K; ++k) {
-    eci_lane[2 * k] = 0;
-    eci_lane[2 * k + 1] = -1;
-  }
-  std::vector<int> lo_seen(K, 33), hi_seen(K, -1);
-  for (int l = 0; l < 32; ++l) {
-    const int lo = lane_term[l], hi = lane_term[l + 1];
-    if (lo >= hi) continue;
-    first[l] = d->term_eci[lo];
-    n_slots = std::max(n_slots, d->term_eci[hi - 1] - first[l] + 1);
-    for (int i = lo; i < hi; ++i) {
-      const int k = d->term_eci[i];
-      lo_seen[k] = std::min(lo_seen[k], l);
-      hi_seen[k] = std::max(hi_seen[k], l);
+  std::vector<uint16_t> terms(4 * (size_t)std::max(T, 1), 0);
+  for (int q = 0; q < G; ++q) {
+    const int t0 = gterm[q], Tg = gterm[q + 1] - gterm[q];
+    int32_t *lt = lane_term.data() + 33 * q, *fi = first.data() + 32 * q, *el = eci_lane.data() + 2 * (size_t)K * q;
+    for (int l = 0; l <= 32; ++l) lt[l] = t0 + (int32_t)(((long long)l * Tg) / 32);
+    for (int k = 0; k < K; ++k) {
+      el[2 * k] = 0;
+      el[2 * k + 1] = -1;
     }
+    std::vector<int> lo_seen(K, 33), hi_seen(K, -1);
+    for (int l = 0; l < 32; ++l) {
+      const int lo = lt[l], hi = lt[l + 1];
+      if (lo >= hi) continue;
+      fi[l] = d->term_eci[lo];
+      n_slots = std::max(n_slots, d->term_eci[hi - 1] - fi[l] + 1);
+      for (int i = lo; i < hi; ++i) {
+        const int k = d->term_eci[i];
+        lo_seen[k] = std::min(lo_seen[k], l);
+        hi_seen[k] = std::max(hi_seen[k], l);
+      }
+    }
+    for (int k = 0; k < K; ++k)
+      if (hi_seen[k] >= 0) {
+        el[2 * k] = lo_seen[k];
+        el[2 * k + 1] = hi_seen[k];
+      }
+    for (int l = 0; l < 32; ++l)
+      for (int i = lt[l]; i < lt[l + 1]; ++i) {
+        const int slot = d->term_eci[i] - fi[l];
+        terms[4 * i] = (uint16_t)((one_idx + 1 + d->term_ref[i]) | (slot << cemc::kRefBits));
+        for (int j = 0; j < 3; ++j)
+          terms[4 * i + 1 + j] = (uint16_t)(j < d->term_size[i] - 1 ? d->term_nb[3 * i + j] : one_idx);
+      }
   }
   if (n_slots > cemc::kMaxSlots) return fail(CEMC_ERR_LIMIT, "a lane chunk spans %d ECIs", n_slots);
-  for (int k = 0; k < K; ++k)
-    if (hi_seen[k] >= 0) {
-      eci_lane[2 * k] = lo_seen[k];
-      eci_lane[2 * k + 1] = hi_seen[k];
-    }
-  std::vector<uint16_t> terms(4 * (size_t)std::max(T, 1), 0);
   std::vector<uint8_t> fterms(8 * (size_t)std::max(T, 1), 0);
-  for (int l = 0; l < 32; ++l)
-    for (int i = lane_term[l]; i < lane_term[l + 1]; ++i) {
-      const int slot = d->term_eci[i] - first[l];
-      terms[4 * i] = (uint16_t)((one_idx + 1 + d->term_ref[i]) | (slot << cemc::kRefBits));
-      for (int j = 0; j < 3; ++j)
-        terms[4 * i + 1 + j] = (uint16_t)(j < d->term_size[i] - 1 ? d->term_nb[3 * i + j] : one_idx);
-    }
   for (int i = 0; i < T; ++i) {
     for (int j = 0; j < 3; ++j) {
       const bool has = j < d->term_size[i] - 1;
@@ -162,14 +194,15 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
     fterms[8 * i + 6] = (uint8_t)d->term_ref[i];
     fterms[8 * i + 7] = (uint8_t)d->term_size[i];
   }
-  std::vector<int32_t> fterm_off(K + 1, 0);
-  {
-    int t = 0;
+  // Term range of each (group, ECI): fterm_off[q * (K + 1) + k].
+  std::vector<int32_t> fterm_off((size_t)G * (K + 1), 0);
+  for (int q = 0; q < G; ++q) {
+    int t = gterm[q];
     for (int k = 0; k < K; ++k) {
-      fterm_off[k] = t;
-      while (t < T && d->term_eci[t] == k) ++t;
+      fterm_off[(size_t)q * (K + 1) + k] = t;
+      while (t < gterm[q + 1] && d->term_eci[t] == k) ++t;
     }
-    fterm_off[K] = T;
+    fterm_off[(size_t)q * (K + 1) + K] = gterm[q + 1];
   }
   // Table form of the trial energy change: the terms grouped by cluster geometry
   // (the ordered member columns of a sub-cluster with the changed site as
@@ -177,15 +210,21 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   // share a pattern, and each chain's kernel tabulates per pattern
   // F(old, new, member species) = sum over its terms of coef * (bf[d_ref][new] -
   // bf[d_ref][old]) * prod bf[d_j][s_j], so a flip costs one lookup per geometry.
+  // With several translation groups each group has its own geometry range
+  // (geo_start) and the groups share patterns; the table stores group 0's
+  // weights, so it needs equal group sizes.
   std::vector<uint32_t> geo_list;  // per geometry: {packed columns, F offset, stride S^m, 0}
   std::vector<int32_t> pat_info;   // per pattern: {m, F offset, first term, end term}
   std::vector<int32_t> pat_terms;  // k | d_ref << 8 | d1 << 12 | d2 << 16 | d3 << 20
+  std::vector<int32_t> geo_start(G + 1, 0);
   int n_geo = 0, n_pat = 0, tab_len = 0;
-  bool table_ok = C < 255 && S <= 8;
-  if (table_ok) {
+  bool table_ok = C < 255 && S <= 8 && equal_groups;
+  std::map<std::vector<std::array<int, 5>>, int> pats;
+  for (int q = 0; q < G && table_ok; ++q) {
+    geo_start[q] = (int)(geo_list.size() / 4);
     std::map<std::vector<int>, std::vector<std::array<int, 5>>> geos;  // member columns -> terms
     std::vector<std::vector<int>> geo_order;
-    for (int t = 0; t < T; ++t) {
+    for (int t = gterm[q]; t < gterm[q + 1]; ++t) {
       const int m = d->term_size[t] - 1;
       std::vector<int> cols(m);
       std::array<int, 5> term{d->term_eci[t], d->term_ref[t], 0, 0, 0};
@@ -200,7 +239,6 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       }
       it->second.push_back(term);
     }
-    std::map<std::vector<std::array<int, 5>>, int> pats;
     for (const auto &cols : geo_order) {
       std::vector<std::array<int, 5>> sig = geos[cols];
       std::sort(sig.begin(), sig.end());
@@ -224,10 +262,11 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       for (int j = 0; j < m; ++j) stride *= S;
       geo_list.insert(geo_list.end(), {packed, (uint32_t)pat_info[4 * id + 1], (uint32_t)stride, 0u});
     }
-    n_geo = (int)geo_order.size();
-    n_pat = (int)pats.size();
-    if (tab_len > cemc::kMaxTable || n_geo > cemc::kMaxGeo) table_ok = false;
   }
+  n_geo = (int)(geo_list.size() / 4);
+  n_pat = (int)pats.size();
+  geo_start[G] = n_geo;
+  if (tab_len > cemc::kMaxTable || n_geo > cemc::kMaxGeo) table_ok = false;
   if (geo_list.empty()) geo_list.assign(4, 0u);
   if (pat_info.empty()) pat_info.assign(4, 0);
   if (pat_terms.empty()) pat_terms.assign(1, 0);
@@ -264,7 +303,7 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   std::vector<int32_t> half_lane_term(17, 0), half_lane_first(16, 0);  // the same terms over 16 lanes
   std::vector<uint8_t> half_shift;
   int minus_id = -1, singlet_eci = -1;
-  bool spin_ok = (B == 1 && S == 2 && C <= CEMC_SPIN_MAX_COLS);
+  bool spin_ok = (B == 1 && S == 2 && C <= CEMC_SPIN_MAX_COLS && G == 1);
   if (spin_ok) {
     if (d->bf[0] == 1.0 && d->bf[1] == -1.0)
       minus_id = 1;
@@ -344,8 +383,8 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   };
   std::vector<Part> parts = {
       {table_pad.data(), sizeof(int32_t) * N * cpad, 0}, {table_cm.data(), sizeof(int32_t) * N * C, 0},
-      {terms.data(), terms.size() * 2, 0},         {lane_term.data(), 33 * 4, 0},
-      {first.data(), 32 * 4, 0},                   {eci_lane.data(), eci_lane.size() * 4, 0},
+      {terms.data(), terms.size() * 2, 0},         {lane_term.data(), lane_term.size() * 4, 0},
+      {first.data(), first.size() * 4, 0},         {eci_lane.data(), eci_lane.size() * 4, 0},
       {d->eci_kind, sizeof(int32_t) * K, 0},       {d->eci_dec, sizeof(int32_t) * K, 0},
       {w.data(), sizeof(double) * K, 0},           {fw.data(), sizeof(double) * K, 0},
       {d->bf, sizeof(double) * B * S, 0},          {fterms.data(), fterms.size(), 0},
@@ -363,6 +402,9 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {pat_terms.data(), pat_terms.size() * 4, 0},
       {movable.data(), movable.size() * 4, 0},
       {site_active.data(), site_active.size(), 0},
+      {sgroup.data(), sgroup.size(), 0},
+      {geo_start.data(), geo_start.size() * 4, 0},
+      {gscale.data(), gscale.size() * 8, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -419,6 +461,10 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.n_movable = n_movable;
   g.movable = reinterpret_cast<const int32_t *>(base + parts[24].off);
   g.site_active = n_movable == N ? nullptr : reinterpret_cast<const int8_t *>(base + parts[25].off);
+  g.n_groups = G;
+  g.site_group = reinterpret_cast<const int8_t *>(base + parts[26].off);
+  g.geo_start = reinterpret_cast<const int32_t *>(base + parts[27].off);
+  g.group_scale = reinterpret_cast<const double *>(base + parts[28].off);
   g.pm1_minus = -1;
   if (B == 1 && S == 2) {
     if (d->bf[0] == 1.0 && d->bf[1] == -1.0) g.pm1_minus = 1;
@@ -481,10 +527,12 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
   const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
   if (want_spin && !geo->spin_ok)
-    return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1 and <= 64 columns");
+    return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1, <= 64 columns and "
+                              "one translation-symmetry group");
   const bool use_spin = want_spin || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
   if (r->kernel == CEMC_KERNEL_TABLE && !g.table_ok)
-    return fail(CEMC_ERR_LIMIT, "the table kernel's pattern tables exceed %d entries", cemc::kMaxTable);
+    return fail(CEMC_ERR_LIMIT, "the table kernel needs translation groups of equal size and pattern tables of at "
+                                "most %d entries", cemc::kMaxTable);
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
     return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs single-site flips with at most 16 cluster ECIs");

@@ -81,11 +81,13 @@ __global__ void __launch_bounds__(kCfThreads) recompute_partial(DevGeo g, const 
   }
   const int me = valid ? occ[i] : 0;
   const int me_bit = (me == minus) ? 1 : 0;
+  // the term ranges of the site's translation group
+  const int32_t *foff = g.fterm_off + (size_t)(valid && g.n_groups > 1 ? g.site_group[i] : 0) * (g.n_eci + 1);
   __syncthreads();
   for (int k = 0; k < g.n_eci; ++k) {
     const int kind = g.eci_kind[k];
     if (kind == 0) continue;
-    const int f0 = g.fterm_off[k], f1 = g.fterm_off[k + 1];
+    const int f0 = foff[k], f1 = foff[k + 1];
     double s;
     if (PM1) {
       int cnt = 0;
@@ -173,7 +175,7 @@ __global__ void energy_kernel(int n_chains, int n_eci, int n_sites, const double
 // ---------------------------------------------------------------------------
 // Single-warp FP64 kernels over explicit moves.
 struct WarpLayout {
-  size_t terms, lane, kind, coef, bf, va, vb, part, d, total;
+  size_t terms, lane, gscale, kind, coef, bf, va, vb, part, d, total;
 };
 
 __host__ __device__ inline WarpLayout warp_layout(const DevGeo &g) {
@@ -181,8 +183,10 @@ __host__ __device__ inline WarpLayout warp_layout(const DevGeo &g) {
   size_t o = 0;
   L.terms = o;
   o = align16(o + 8 * (size_t)g.n_terms);
-  L.lane = o;
-  o = align16(o + 4 * (size_t)(33 + 32 + 2 * g.n_eci));
+  L.lane = o;  // one block of lane-chunk tables per translation group
+  o = align16(o + 4 * (size_t)g.n_groups * group_lane_ints(g.n_eci));
+  L.gscale = o;
+  o = align16(o + 8 * (size_t)g.n_groups);
   L.kind = o;
   o = align16(o + 2 * (size_t)g.n_eci);
   L.coef = o;
@@ -205,9 +209,9 @@ size_t warp_kernel_smem(const DevGeo &g) { return warp_layout(g).total; }
 
 struct WarpSmem {
   uint16_t *terms;
-  int32_t *lane_term, *first, *eci_lane;
+  int32_t *lane_term;  // [groups][group_lane_ints]
   int8_t *kind, *dec;
-  double *coef, *bf, *va, *vb, *part, *d;
+  double *gscale, *coef, *bf, *va, *vb, *part, *d;
 };
 
 __device__ WarpSmem warp_stage(const DevGeo &g, const double *eci, unsigned char *smem) {
@@ -215,8 +219,7 @@ __device__ WarpSmem warp_stage(const DevGeo &g, const double *eci, unsigned char
   WarpSmem s;
   s.terms = reinterpret_cast<uint16_t *>(smem + L.terms);
   s.lane_term = reinterpret_cast<int32_t *>(smem + L.lane);
-  s.first = s.lane_term + 33;
-  s.eci_lane = s.first + 32;
+  s.gscale = reinterpret_cast<double *>(smem + L.gscale);
   s.kind = reinterpret_cast<int8_t *>(smem + L.kind);
   s.dec = s.kind + g.n_eci;
   s.coef = reinterpret_cast<double *>(smem + L.coef);
@@ -228,14 +231,17 @@ __device__ WarpSmem warp_stage(const DevGeo &g, const double *eci, unsigned char
   const int tid = threadIdx.x;
   for (int i = tid; i < g.n_terms; i += blockDim.x)
     reinterpret_cast<uint2 *>(s.terms)[i] = reinterpret_cast<const uint2 *>(g.terms)[i];
-  for (int i = tid; i < 33; i += blockDim.x) s.lane_term[i] = g.lane_term[i];
-  for (int i = tid; i < 32; i += blockDim.x) s.first[i] = g.lane_first_eci[i];
+  const int LG = group_lane_ints(g.n_eci);
+  for (int i = tid; i < g.n_groups * LG; i += blockDim.x) {
+    const int q = i / LG, r = i - q * LG;
+    s.lane_term[i] = r < 33 ? g.lane_term[33 * q + r]
+                            : (r < 65 ? g.lane_first_eci[32 * q + r - 33] : g.eci_lane[(size_t)2 * g.n_eci * q + r - 65]);
+  }
+  for (int q = tid; q < g.n_groups; q += blockDim.x) s.gscale[q] = g.group_scale[q];
   for (int k = tid; k < g.n_eci; k += blockDim.x) {
     const int kind = g.eci_kind[k];
     s.kind[k] = (int8_t)kind;
     s.dec[k] = (int8_t)g.eci_dec[k];
-    s.eci_lane[2 * k] = g.eci_lane[2 * k];
-    s.eci_lane[2 * k + 1] = g.eci_lane[2 * k + 1];
     s.coef[k] = kind == 2 ? eci[k] * (double)g.n_sites * g.eci_w[k] : (kind == 1 ? eci[k] : 0.0);
   }
   for (int i = tid; i < g.n_bf * g.n_sym; i += blockDim.x) s.bf[i] = g.bf[i];
@@ -261,11 +267,11 @@ __global__ void apply_changes_kernel(DevGeo g, int8_t *occ, double *cf, double *
       break;
     }
     if (o == n) continue;
+    const int grp = g.n_groups > 1 ? g.site_group[site] : 0;
     gather_vals<double>(g, occ, s.bf, site, o, n, -1, 0, s.va, nbr, lane);
     __syncwarp();
-    lane_terms<double, false>(g, s.terms, s.lane_term, s.va, s.vb, s.part, lane);
-    __syncwarp();
-    eci_changes<double, false>(g, s.eci_lane, s.first, s.kind, s.dec, s.coef, s.part, s.va, s.vb, s.d, lane);
+    site_changes<double, false>(g, s.terms, s.lane_term, s.kind, s.dec, s.coef, s.gscale, s.part, s.va, s.vb, s.d, grp,
+                                grp, lane);
     for (int k = lane; k < g.n_eci; k += 32) {
       const int kind = s.kind[k];
       if (kind == 2) cf[k] = cf[k] + s.d[k] * g.eci_w[k];
@@ -290,21 +296,21 @@ __global__ void delta_e_kernel(DevGeo g, const int8_t *occ, const double *eci, i
   const int lane = threadIdx.x;
   int nbra[4], nbrb[4];
   double de;
+  const int ga = g.n_groups > 1 ? g.site_group[site_a] : 0;
   if (move == CEMC_MOVE_SWAP) {
     const int A = occ[site_a], B = occ[site_b];
+    const int gb = g.n_groups > 1 ? g.site_group[site_b] : 0;
     gather_vals<double>(g, occ, s.bf, site_a, A, B, -1, 0, s.va, nbra, lane);
     gather_vals<double>(g, occ, s.bf, site_b, B, A, site_a, B, s.vb, nbrb, lane);
     __syncwarp();
-    lane_terms<double, true>(g, s.terms, s.lane_term, s.va, s.vb, s.part, lane);
-    __syncwarp();
-    de = eci_changes<double, true>(g, s.eci_lane, s.first, s.kind, s.dec, s.coef, s.part, s.va, s.vb, s.d, lane);
+    de = site_changes<double, true>(g, s.terms, s.lane_term, s.kind, s.dec, s.coef, s.gscale, s.part, s.va, s.vb, s.d,
+                                    ga, gb, lane);
   } else {
     const int A = occ[site_a];
     gather_vals<double>(g, occ, s.bf, site_a, A, new_a, -1, 0, s.va, nbra, lane);
     __syncwarp();
-    lane_terms<double, false>(g, s.terms, s.lane_term, s.va, s.vb, s.part, lane);
-    __syncwarp();
-    de = eci_changes<double, false>(g, s.eci_lane, s.first, s.kind, s.dec, s.coef, s.part, s.va, s.vb, s.d, lane);
+    de = site_changes<double, false>(g, s.terms, s.lane_term, s.kind, s.dec, s.coef, s.gscale, s.part, s.va, s.vb,
+                                     s.d, ga, ga, lane);
   }
   __syncwarp();
   for (int k = lane; k < g.n_eci; k += 32) {

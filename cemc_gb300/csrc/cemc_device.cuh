@@ -56,7 +56,19 @@ struct DevGeo {
   int n_movable;             // sites that may change (n_sites when there is no background)
   const int32_t *movable;    // [n_movable] ascending (used when n_movable < n_sites)
   const int8_t *site_active; // [n_sites] 1 = movable; NULL when every site is
+  // Translation-symmetry groups (1 = one group).  The lane-chunk tables
+  // (lane_term [G][33], lane_first_eci [G][32], eci_lane [G][2 n_eci]) and
+  // fterm_off ([G][n_eci + 1]) hold one block per group; a site's table row
+  // lists its group's columns.
+  int n_groups;
+  const int8_t *site_group;    // [n_sites]
+  const int32_t *geo_start;    // [n_groups + 1] table-form geometry range of each group
+  const double *group_scale;   // [n_groups] factor on a site's cluster-ECI changes
 };
+
+// Ints of one group's block of lane-chunk tables in shared memory:
+// [33] chunk bounds, [32] first ECI per lane, [2 n_eci] lane range per ECI.
+__host__ __device__ inline int group_lane_ints(int n_eci) { return 65 + 2 * n_eci; }
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -210,13 +222,14 @@ __device__ __forceinline__ void lane_terms(const DevGeo &g, const uint16_t *term
   part[cur * 32 + lane] = acc;
 }
 
-// Combine per-lane partials into the per-ECI change D[k] (unweighted term sum
-// for cluster ECIs, delta[d] for singlets) and return the energy change
-// sum_k coef[k] * D[k] (coef = N * eci * weight), identical on all lanes.
-template <typename R, bool TWO>
+// Combine per-lane partials into the per-ECI change D[k] (term sum times the
+// site group's scale for cluster ECIs, delta[d] for singlets) and return the
+// energy change sum_k coef[k] * D[k] (coef = N * eci * weight), identical on
+// all lanes.  ADD adds to D instead of overwriting it.
+template <typename R, bool TWO, bool ADD = false>
 __device__ __forceinline__ R eci_changes(const DevGeo &g, const int32_t *eci_lane_s, const int32_t *first_s,
                                          const int8_t *kind_s, const int8_t *dec_s, const R *coef_s, const R *part,
-                                         const R *va, const R *vb, R *D, int lane) {
+                                         const R *va, const R *vb, R *D, int lane, R gscale = (R)1) {
   R de = (R)0;
   for (int k = lane; k < g.n_eci; k += 32) {
     R v = (R)0;
@@ -224,15 +237,44 @@ __device__ __forceinline__ R eci_changes(const DevGeo &g, const int32_t *eci_lan
     if (kind == 2) {
       const int lo = eci_lane_s[2 * k], hi = eci_lane_s[2 * k + 1];
       for (int l = lo; l <= hi; ++l) v += part[(k - first_s[l]) * 32 + l];
+      v *= gscale;
     } else if (kind == 1) {
       const int d = dec_s[k];
       v = va[g.one_idx + 1 + d];
       if (TWO) v += vb[g.one_idx + 1 + d];
     }
-    D[k] = v;
+    D[k] = ADD ? D[k] + v : v;
     de += coef_s[k] * v;
   }
   return warp_sum(de);
+}
+
+// Energy change and per-ECI changes D of one flip (va) or swap (va, then vb
+// with the first site already changed) whose sites belong to translation
+// groups ga and gb.  lane_s holds the groups' lane-chunk blocks
+// (group_lane_ints each), gscale_s their scales.  Two sites of one group walk
+// the group's terms once for both vals arrays; two groups take one pass each.
+template <typename R, bool SWAP>
+__device__ __forceinline__ R site_changes(const DevGeo &g, const uint16_t *terms_s, const int32_t *lane_s,
+                                          const int8_t *kind_s, const int8_t *dec_s, const R *coef_s,
+                                          const R *gscale_s, R *part, const R *va, const R *vb, R *D, int ga, int gb,
+                                          int lane) {
+  const int LG = group_lane_ints(g.n_eci);
+  const int32_t *la = lane_s + ga * LG;
+  if (!SWAP || ga == gb) {
+    lane_terms<R, SWAP>(g, terms_s, la, va, vb, part, lane);
+    __syncwarp();
+    return eci_changes<R, SWAP>(g, la + 65, la + 33, kind_s, dec_s, coef_s, part, va, vb, D, lane, gscale_s[ga]);
+  }
+  const int32_t *lb = lane_s + gb * LG;
+  lane_terms<R, false>(g, terms_s, la, va, va, part, lane);
+  __syncwarp();
+  R de = eci_changes<R, false>(g, la + 65, la + 33, kind_s, dec_s, coef_s, part, va, va, D, lane, gscale_s[ga]);
+  __syncwarp();
+  lane_terms<R, false>(g, terms_s, lb, vb, vb, part, lane);
+  __syncwarp();
+  de += eci_changes<R, false, true>(g, lb + 65, lb + 33, kind_s, dec_s, coef_s, part, vb, vb, D, lane, gscale_s[gb]);
+  return de;
 }
 
 }  // namespace cemc

@@ -60,7 +60,7 @@ struct Draw {
 };
 
 struct McLayout {
-  size_t cf, eci, w, acc, cfw, coef, bf, terms, lane_term, kind, misc;
+  size_t cf, eci, w, acc, cfw, coef, bf, terms, lane_term, kind, misc, grp;
   size_t sp_eci, sp_masks, sp_shift, sp_lane;  // spin-basis tables (empty unless n_cl > 0)
   // per-round trial records (two buffers, by round parity), kRoundSlots entries each
   size_t rec, rec_stride, rec_sa, rec_sb, rec_de, rec_ds, rec_acc, rec_la, rec_lb, rec_A, rec_B;
@@ -105,12 +105,14 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + (size_t)rsize * g.n_bf * g.n_sym);
   L.terms = o;
   o = align16(o + 8 * (size_t)g.n_terms);
-  L.lane_term = o;
-  o = align16(o + 4 * (size_t)(33 + 32 + 2 * K));
+  L.lane_term = o;  // one block of lane-chunk tables per translation group
+  o = align16(o + 4 * (size_t)(g.n_groups > 1 ? g.n_groups : 1) * group_lane_ints(g.n_eci));
   L.kind = o;
   o = align16(o + 2 * K);
   L.misc = o;
   o = align16(o + 4 * 64);
+  L.grp = o;  // per translation group: scale (as R), then the table-form geometry ranges
+  o = align16(o + 8 * CEMC_MAX_GROUPS + 4 * (CEMC_MAX_GROUPS + 1));
   L.sp_eci = o;
   o = align16(o + 32 * (size_t)n_cl);
   L.sp_masks = o;  // per multi-site term: {mask lo, mask hi, 32-lane shift, 16-lane shift}

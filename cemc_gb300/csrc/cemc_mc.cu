@@ -148,12 +148,13 @@ __device__ __forceinline__ void table_gather(const DevGeo &g, const int8_t *occ,
 // Energy change of one flip (or, TWO, of a swap's two flips) from the pattern
 // tables: one lookup per cluster geometry, F[off + on * S^m + s1 + S s2 + S^2 s3]
 // with on = old * S + new and the member species s_j of the geometry's columns.
+// Geometries [lo, hi) are those of the changed site's translation group.
 template <typename R, bool TWO>
 __device__ __forceinline__ R table_de(const DevGeo &g, const uint4 *geos, const R *F, const int8_t *spa,
-                                      const int8_t *spb, int on_a, int on_b, int lane) {
+                                      const int8_t *spb, int on_a, int on_b, int lo, int hi, int lane) {
   const int S = g.n_sym, S2 = S * S;
   R sum = (R)0;
-  for (int i = lane; i < g.n_geo; i += 32) {
+  for (int i = lo + lane; i < hi; i += 32) {
     const uint4 e = geos[i];
     const int c1 = e.x & 0xff, c2 = (e.x >> 8) & 0xff, c3 = (e.x >> 16) & 0xff;
     sum += F[e.y + on_a * e.z + spa[c1] + S * spa[c2] + S2 * spa[c3]];
@@ -253,9 +254,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   R *coef_s = reinterpret_cast<R *>(smem + L.coef);
   R *bf_s = reinterpret_cast<R *>(smem + L.bf);
   uint16_t *terms_s = reinterpret_cast<uint16_t *>(smem + L.terms);
-  int32_t *lane_term_s = reinterpret_cast<int32_t *>(smem + L.lane_term);
-  int32_t *first_s = lane_term_s + 33;
-  int32_t *eci_lane_s = first_s + 32;
+  int32_t *lane_term_s = reinterpret_cast<int32_t *>(smem + L.lane_term);  // [groups][group_lane_ints]
+  R *gscale_s = reinterpret_cast<R *>(smem + L.grp);                          // [groups]
+  int32_t *gstart_s = reinterpret_cast<int32_t *>(smem + L.grp + 8 * CEMC_MAX_GROUPS);  // [groups + 1]
   int8_t *kind_s = reinterpret_cast<int8_t *>(smem + L.kind);
   int8_t *dec_s = kind_s + n_eci;
   // misc: [1] status, [2] species present, [4..12) present ids, [12..20) site-list
@@ -312,12 +313,18 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     coef_s[k] = (R)(kind == 2 ? e * (double)N * g.eci_w[k] : (kind == 1 ? e : 0.0));
     kind_s[k] = (int8_t)kind;
     dec_s[k] = (int8_t)g.eci_dec[k];
-    eci_lane_s[2 * k] = g.eci_lane[2 * k];
-    eci_lane_s[2 * k + 1] = g.eci_lane[2 * k + 1];
   }
   for (int i = tid; i < g.n_bf * g.n_sym; i += blockDim.x) bf_s[i] = (R)g.bf[i];
-  for (int i = tid; i < 33; i += blockDim.x) lane_term_s[i] = g.lane_term[i];
-  for (int i = tid; i < 32; i += blockDim.x) first_s[i] = g.lane_first_eci[i];
+  {
+    const int LG = group_lane_ints(n_eci);
+    for (int i = tid; i < g.n_groups * LG; i += blockDim.x) {
+      const int q = i / LG, r = i - q * LG;
+      lane_term_s[i] = r < 33 ? g.lane_term[33 * q + r]
+                              : (r < 65 ? g.lane_first_eci[32 * q + r - 33] : g.eci_lane[(size_t)2 * n_eci * q + r - 65]);
+    }
+    for (int q = tid; q < g.n_groups; q += blockDim.x) gscale_s[q] = (R)g.group_scale[q];
+    for (int q = tid; q <= g.n_groups; q += blockDim.x) gstart_s[q] = g.geo_start[q];
+  }
   {
     const uint2 *src = reinterpret_cast<const uint2 *>(g.terms);
     uint2 *dst = reinterpret_cast<uint2 *>(terms_s);
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       d.w1 = w0.v[1];
       d.w2 = w0.v[2];
       d.w3 = w0.v[3];
-      d.pad = 0;
+      d.pad = 0;  // flips: the site's translation group
       if (SWAP) {
         const cemc_u32x4 w1 = cemc_trial_draw(a.seed, key, t, 1);
         d.x0 = w1.v[0];
@@ -451,6 +458,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         // the flipped site: uniform over the movable sites (all sites without a background)
         d.site = g.n_movable == N ? (int)cemc_below(w0.v[0], (uint32_t)N)
                                   : g.movable[cemc_below(w0.v[0], (uint32_t)g.n_movable)];
+        if (g.n_groups > 1) d.pad = (uint32_t)g.site_group[d.site];
         const int32_t *src = g.table + (size_t)d.site * cpad;
         int32_t *dst = rows + (size_t)slot * cpad;
         for (int q = 0; q < cpad; q += 4) cp_async16(dst + q, src + q);
@@ -827,23 +835,37 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           }
           R de;
           int delta = 0;
+          // translation groups of the changed sites (the spin form has one group)
+          int ga = 0, gb = 0;
+          if (!SPIN && g.n_groups > 1) {
+            if (!SWAP) {
+              ga = (int)dr.pad;
+            } else {
+              ga = g.site_group[sa];
+              gb = g.site_group[sb];
+            }
+          }
           if constexpr (TAB) {
             __syncwarp();
             const int S = g.n_sym;
             if (!SWAP) {
-              de = table_de<R, false>(g, geos_s, ftab, sp_a, sp_b, old_a * S + na, 0, lane);
+              de = table_de<R, false>(g, geos_s, ftab, sp_a, sp_b, old_a * S + na, 0, gstart_s[ga], gstart_s[ga + 1],
+                                      lane);
               for (int b = 0; b < g.n_bf; ++b)
                 if (g.singlet_eci[b] >= 0)
                   de += coef_s[g.singlet_eci[b]] * (bf_s[b * S + na] - bf_s[b * S + old_a]);
+            } else if (ga == gb) {
+              de = table_de<R, true>(g, geos_s, ftab, sp_a, sp_b, A_ * S + B_, B_ * S + A_, gstart_s[ga],
+                                     gstart_s[ga + 1], lane);
             } else {
-              de = table_de<R, true>(g, geos_s, ftab, sp_a, sp_b, A_ * S + B_, B_ * S + A_, lane);
+              de = table_de<R, false>(g, geos_s, ftab, sp_a, sp_a, A_ * S + B_, 0, gstart_s[ga], gstart_s[ga + 1], lane) +
+                   table_de<R, false>(g, geos_s, ftab, sp_b, sp_b, B_ * S + A_, 0, gstart_s[gb], gstart_s[gb + 1], lane);
             }
             __syncwarp();
           } else if constexpr (!SPIN) {
             __syncwarp();
-            lane_terms<R, SWAP>(g, terms_s, lane_term_s, va, vb, part, lane);
-            __syncwarp();
-            de = eci_changes<R, SWAP>(g, eci_lane_s, first_s, kind_s, dec_s, coef_s, part, va, vb, Dw, lane);
+            de = site_changes<R, SWAP>(g, terms_s, lane_term_s, kind_s, dec_s, coef_s, gscale_s, part, va, vb, Dw, ga,
+                                       gb, lane);
             __syncwarp();
           } else {
             // P_k = sum over the terms of cluster ECI k of the product of the other

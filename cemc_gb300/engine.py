@@ -58,12 +58,13 @@ class Geometry:
     def __init__(self, model: CEModel, device="cuda"):
         self.device = require_cuda(device)
         if not model.gpu_supported:
-            raise NotImplementedError("the GPU path handles one translation-symmetry group with at most 4 decorations")
+            raise NotImplementedError("the GPU path handles at most %d translation-symmetry groups and 4 decorations"
+                                      % _lib.MAX_GROUPS)
         self.model = model
         self.L = _lib.load()
         m = model
         self._host = {
-            "table": np.ascontiguousarray(m.table, dtype=np.int32),
+            "table": np.ascontiguousarray(m.gpu_table, dtype=np.int32),
             "bf": np.ascontiguousarray(m.bf, dtype=np.float64),
             "eci_kind": np.ascontiguousarray(m.eci_kind, dtype=np.int32),
             "eci_dec": np.ascontiguousarray(m.eci_dec, dtype=np.int32),
@@ -74,13 +75,18 @@ class Geometry:
             "term_size": np.ascontiguousarray(m.term_size, dtype=np.int32),
             "term_nb": np.ascontiguousarray(m.term_nb, dtype=np.int32),
             "movable": np.ascontiguousarray(m.movable, dtype=np.int32),
+            "site_group": np.ascontiguousarray(m.site_group, dtype=np.int32),
+            "group_terms": np.ascontiguousarray(m.group_terms, dtype=np.int32),
+            "group_scale": np.ascontiguousarray(m.group_scale, dtype=np.float64),
         }
         h = self._host
-        desc = _lib.GeometryDesc(m.n_sites, m.n_cols, m.n_sym, m.n_bf, m.n_eci, m.n_terms,
+        desc = _lib.GeometryDesc(m.n_sites, m.gpu_n_cols, m.n_sym, m.n_bf, m.n_eci, m.n_terms,
                                  *[h[n].ctypes.data for n in ("table", "bf", "eci_kind", "eci_dec", "eci_weight",
                                                               "eci_full_weight", "term_eci", "term_ref",
                                                               "term_size", "term_nb")],
-                                 h["movable"].ctypes.data, int(len(m.movable)))
+                                 h["movable"].ctypes.data, int(len(m.movable)), int(m.n_groups),
+                                 h["site_group"].ctypes.data, h["group_terms"].ctypes.data,
+                                 h["group_scale"].ctypes.data)
         handle = C.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.L.cemc_geometry_create(C.byref(desc), C.byref(handle)))

@@ -490,3 +490,231 @@ def seeded_ecis(cset: ClusterSet, seed: int, c0: float = -3.0, singlet_sigma: fl
             else:
                 eci[e.name] = float(rng.normal(0.0, quad_sigma))
     return eci
+
+
+# ---------------------------------------------------------------------------
+# Several translation-symmetry groups: the FCC lattice under the symmetry of
+# its L1_2 (Cu3Au-type) ordering, space group Pm-3m.  Its translations are the
+# cubic lattice vectors (even vectors in half-lattice units) and its point
+# group is O_h about a cube corner, so the four sites of the conventional cube
+# fall into four translation classes: the corner sublattice and three face
+# sublattices.  The reference takes such settings from CLEASE (one
+# ``cluster_info`` dict and one ``ref_indx`` per group; its tests build a
+# four-group crystal in tests/helper_functions.py:8-27) and keeps one cluster
+# list per group (cpp/src/ce_updater.cpp:115-148): a cluster type seen from
+# several groups keeps one name, and ``M_prefix`` sums its sub-cluster counts
+# over the groups.
+
+
+def _canonical_key_sg(points: np.ndarray, tmod: int) -> Tuple:
+    """Key of a point set's orbit under translations by ``tmod * Z^3`` and O_h about the origin."""
+    best = None
+    for g in _OH:
+        img = points @ g.T
+        for q in img:
+            t = q - np.mod(q, tmod)
+            key = tuple(sorted(map(tuple, (img - t).tolist())))
+            if best is None or key < best:
+                best = key
+    return best
+
+
+def _space_group_maps(src: np.ndarray, dst: np.ndarray, tmod: int):
+    """Yield ``mapping`` (index of src point -> index of dst point) of every space-group element src -> dst."""
+    dst_set = {tuple(p): q for q, p in enumerate(dst.tolist())}
+    n = len(src)
+    for g in _OH:
+        img = src @ g.T
+        for p0 in dst:
+            t = p0 - img[0]
+            if np.any(np.mod(t, tmod)):
+                continue
+            mapping = [dst_set.get(tuple(p)) for p in (img + t).tolist()]
+            if None in mapping or len(set(mapping)) != n:
+                continue
+            yield mapping
+
+
+def _map_onto_sg(points: np.ndarray, proto: np.ndarray, tmod: int) -> List[int]:
+    """``order[q]`` = index into ``points`` of the site that prototype position ``q`` corresponds to."""
+    for mapping in _space_group_maps(points, proto, tmod):
+        order = [0] * len(points)
+        for idx, q in enumerate(mapping):
+            order[q] = idx
+        return order
+    raise RuntimeError("sub-cluster is not equivalent to its prototype")
+
+
+def _equiv_sites_sg(proto: np.ndarray, tmod: int) -> List[List[int]]:
+    """Orbits (size >= 2) of the prototype's stabiliser in the space group, on its positions."""
+    n = len(proto)
+    parent = list(range(n))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for mapping in _space_group_maps(proto, proto, tmod):
+        for q in range(n):
+            a, b = find(q), find(mapping[q])
+            if a != b:
+                parent[a] = b
+    groups: Dict[int, List[int]] = {}
+    for q in range(n):
+        groups.setdefault(find(q), []).append(q)
+    return [sorted(gq) for gq in sorted(groups.values()) if len(gq) >= 2]
+
+
+@dataclass
+class SublatticeClusterType:
+    """One cluster type (space-group orbit) with its sub-clusters per translation group."""
+
+    name: str
+    size: int
+    dia2: int
+    prototype: np.ndarray
+    equiv_sites: List[List[int]]
+    members: List[List[np.ndarray]]  # [group] -> list of (size-1, 3) member positions around the group's reference
+    orders: List[List[List[int]]]   # [group] -> canonical order of [ref] + members
+
+
+def enumerate_l12_cluster_types(pair_shells: int, triplet_shells: int,
+                                quad_shells: int) -> List[SublatticeClusterType]:
+    """Cluster types of the FCC lattice under Pm-3m, seen from the four sublattice references.
+
+    The reference of group b is basis site b of the cube at the origin.  Size
+    cut-offs follow ``enumerate_cluster_types`` (every pairwise distance of a
+    cluster within the given shell radius).
+    """
+    max_shell = max(pair_shells, triplet_shells, quad_shells, 1)
+    shells = fcc_shell_vectors(max_shell)
+    radii = [int((s[0] * s[0]).sum()) for s in shells]
+    n_groups = len(_FCC_BASIS)
+    types: List[SublatticeClusterType] = []
+    for size, n_shells in ((2, pair_shells), (3, triplet_shells), (4, quad_shells)):
+        if n_shells <= 0:
+            continue
+        cutoff = radii[n_shells - 1]
+        vecs = np.concatenate(shells[:n_shells])
+        found: Dict[Tuple, SublatticeClusterType] = {}
+        for b, ref in enumerate(_FCC_BASIS):
+            for combo in itertools.combinations(range(len(vecs)), size - 1):
+                pts = np.vstack([ref[None, :], ref[None, :] + vecs[list(combo)]])
+                diff = pts[:, None, :] - pts[None, :, :]
+                d2 = (diff * diff).sum(axis=2)
+                if d2.max() > cutoff:
+                    continue
+                key = _canonical_key_sg(pts, 2)
+                ct = found.get(key)
+                if ct is None:
+                    proto = np.array(key, dtype=np.int64)
+                    ct = SublatticeClusterType("", size, int(d2.max()), proto, _equiv_sites_sg(proto, 2),
+                                               [[] for _ in range(n_groups)], [[] for _ in range(n_groups)])
+                    found[key] = ct
+                ct.members[b].append(pts[1:].copy())
+                ct.orders[b].append(_map_onto_sg(pts, ct.prototype, 2))
+        cts = sorted(found.values(),
+                     key=lambda c: (c.dia2, sum(len(m) for m in c.members), c.prototype.tolist()))
+        dias = sorted({c.dia2 for c in cts})
+        variant: Dict[int, int] = {}
+        for c in cts:
+            di = dias.index(c.dia2)
+            v = variant.get(di, 0)
+            variant[di] = v + 1
+            c.name = "c%d_d%04d_%d" % (size, di, v)
+            types.append(c)
+    return types
+
+
+class SublatticeSettings:
+    """Settings object of an FCC supercell with several translation-symmetry groups (L1_2 symmetry).
+
+    Same attribute formats as ``Settings``.  ``index_by_trans_symm`` lists the
+    sites of each group; ``cluster_info`` holds one dict per group whose
+    ``indices`` are the member sites of the sub-clusters around the group's
+    reference site; the translation matrix maps a column site j of site i's
+    group to j + (position of i - position of the group's reference).
+
+    ``group_of_basis`` assigns the four sublattices to groups.  The default
+    (0, 1, 2, 3) gives the four translation classes.  Merging sublattices,
+    e.g. (0, 1, 1, 1), gives groups of unequal size whose members share the
+    cluster list of the group's first sublattice (carried over by an FCC
+    translation): settings the reference accepts, which exercise its
+    per-group normalisation ``M_prefix * N_group`` (ce_updater.cpp:400-402)
+    with N_group differing between groups.
+    """
+
+    def __init__(self, cell: FCCSupercell, types: List[SublatticeClusterType], symbols: Sequence[str],
+                 group_of_basis: Sequence[int] = (0, 1, 2, 3)):
+        self.cell = cell
+        self.unique_elements = sorted(symbols)
+        self.num_unique_elements = len(self.unique_elements)
+        self.cset = ClusterSet(types, self.num_unique_elements - 1)
+        if self.num_unique_elements == 2:
+            self.basis_functions = binary_basis(self.unique_elements)
+        elif self.num_unique_elements == 3:
+            self.basis_functions = ternary_basis(self.unique_elements)
+        else:
+            raise ValueError("only binary and ternary alloys are generated")
+        n = cell.n_sites
+        gob = np.asarray(group_of_basis, dtype=np.int64)
+        n_groups = int(gob.max()) + 1
+        if sorted(set(gob.tolist())) != list(range(n_groups)) or len(gob) != len(_FCC_BASIS):
+            raise ValueError("group_of_basis must map the four sublattices onto groups 0..n-1")
+        ref_basis = [int(np.nonzero(gob == q)[0][0]) for q in range(n_groups)]  # a group's first sublattice
+        self.n_sites = n
+        basis_of = np.arange(n) % len(_FCC_BASIS)  # site order: 4 basis sites per cube
+        self.site_basis = basis_of
+        self.index_by_trans_symm = [np.nonzero(gob[basis_of] == q)[0].tolist() for q in range(n_groups)]
+        self.background_indices: List[int] = []
+        info: List[Dict[str, dict]] = []
+        col_set = set()
+        for b in ref_basis:
+            d: Dict[str, dict] = {}
+            for t in types:
+                if not t.members[b]:
+                    continue
+                idx = [cell.index_of(m).astype(np.int64).tolist() for m in t.members[b]]
+                for row, m in zip(idx, t.members[b]):
+                    if len(set(row)) != len(row) or b in row:
+                        raise ValueError("supercell too small: cluster members alias onto the same site")
+                col_set.update(x for row in idx for x in row)
+                d[t.name] = {
+                    "ref_indx": b,
+                    "size": t.size,
+                    "max_cluster_dia": 0.5 * cell.a * math.sqrt(t.dia2),
+                    "symm_group": b,
+                    "name": t.name,
+                    "descriptor": "l12_%d_body_d2_%d" % (t.size, t.dia2),
+                    "indices": idx,
+                    "order": [list(o) for o in t.orders[b]],
+                    "equiv_sites": [list(g) for g in t.equiv_sites],
+                }
+            info.append(d)
+        self.cluster_info = info
+        cols = np.array(sorted(col_set), dtype=np.int64)
+        self.column_sites = cols
+        # every offset that a group's sub-clusters reach must land on a distinct site
+        for b in ref_basis:
+            offs = {tuple((m - _FCC_BASIS[b]).tolist()) for t in types for ms in t.members[b] for m in ms}
+            sites = cell.index_of(np.array(sorted(offs), dtype=np.int64) + _FCC_BASIS[b])
+            if len(set(sites.tolist())) != len(sites):
+                raise ValueError("supercell too small: neighbour offsets alias onto the same site")
+        ref_site = np.array(ref_basis, dtype=np.int64)[gob[basis_of]]  # reference site (cube 0) of i's group
+        shift = cell.positions - cell.positions[ref_site]  # position of i - position of its group's reference
+        self.table = cell.index_of(cell.positions[cols][None, :, :] + shift[:, None, :]).astype(np.int32)
+        self._trans_list = None
+
+    trans_matrix = Settings.trans_matrix
+    symbol_ids = Settings.symbol_ids
+    bf_table = Settings.bf_table
+
+
+def l12_settings(L: int, pair_shells: int, triplet_shells: int, quad_shells: int,
+                 symbols: Sequence[str], a: float = 4.05,
+                 group_of_basis: Sequence[int] = (0, 1, 2, 3)) -> SublatticeSettings:
+    """FCC supercell of ``L^3`` cubes with the sublattices as translation-symmetry groups."""
+    return SublatticeSettings(FCCSupercell(L, a), enumerate_l12_cluster_types(pair_shells, triplet_shells,
+                                                                              quad_shells), symbols, group_of_basis)

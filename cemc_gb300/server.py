@@ -172,7 +172,7 @@ class MCServer:
             eci = seeded_ecis(s.cset, 0)
             m = CEModel(s, list(eci))
             geo = E.Geometry(m, self.device)
-            tbytes = m.n_sites * m.n_cols * 8 + m.n_terms * 16
+            tbytes = m.n_sites * m.gpu_n_cols * 8 + m.n_terms * 16
             self.used += tbytes
             hit = (m, geo, eci)
             self.models[key] = hit

@@ -8,9 +8,10 @@ produces
 
 * the reference-shaped model (per-cluster member columns, canonical order,
   equivalent decorations, normalisation counts), and
-* the flattened "terms" the GPU kernels walk: one term per
-  (cluster ECI, equivalent decoration, sub-cluster), carrying the decoration
-  index of the changed site and (column, decoration) of every other member.
+* the flattened "terms" the GPU kernels walk: one term per (translation
+  group, cluster ECI, equivalent decoration, sub-cluster), carrying the
+  decoration index of the changed site and (column, decoration) of every
+  other member, with the columns in the group's own order (``gpu_table``).
 
 Semantics kept from the reference (``ce_updater.cpp``):
 * ECI names are kept in sorted order (``named_array.cpp:7-23``);
@@ -190,42 +191,78 @@ class CEModel:
         return np.ascontiguousarray(tm[:, cols])
 
     def _build_terms(self):
-        """Flatten (ECI, equivalent decoration, sub-cluster) into GPU terms, sorted by ECI."""
-        term_eci, term_ref, term_size, term_nb = [], [], [], []
+        """Flatten (group, ECI, equivalent decoration, sub-cluster) into GPU terms.
+
+        Terms are sorted by translation group, then ECI.  Each group gets its
+        own column order (the columns its sub-clusters name, ascending), and
+        ``gpu_table`` lists a site's neighbours in its group's order; unused
+        trailing entries point at the site itself, so every row is exactly
+        the site's neighbourhood.  With one group this is the reference's
+        column order and ``gpu_table == table``.
+        """
+        G = self.n_groups
+        self.gpu_supported = self.n_bf <= 4 and 1 <= G <= 8
+        group_cols: List[List[int]] = []
+        for g in range(G):
+            used = set()
+            for t in range(len(self.type_names)):
+                off, m, size = int(self.type_off[t, g]), int(self.type_m[t, g]), int(self.type_size[t])
+                for r in range(off, off + m):
+                    used.update(int(c) for c in self.members[r, :size - 1])
+            group_cols.append(sorted(used))
+        self.group_cols = group_cols
+        n_pack = max([len(c) for c in group_cols] + [1])
+        gpu_table = np.repeat(np.arange(self.n_sites, dtype=np.int32)[:, None], n_pack, axis=1)
+        for g in range(G):
+            sites = np.nonzero(self.site_group == g)[0]
+            cols = group_cols[g]
+            if len(cols):
+                gpu_table[np.ix_(sites, np.arange(len(cols)))] = self.table[np.ix_(sites, np.array(cols))]
+        self.gpu_table = np.ascontiguousarray(gpu_table, dtype=np.int32)
+        self.gpu_n_cols = int(n_pack)
+        n_ref = int(self.group_count[0]) if G else 1
+        self.group_scale = np.array([float(n_ref) / float(max(int(c), 1)) for c in self.group_count]
+                                    if G else [1.0])
+
+        term_eci, term_ref, term_size, term_nb, group_terms = [], [], [], [], [0]
         weight = np.zeros(self.n_eci)
         full_weight = np.zeros(self.n_eci)
-        self.gpu_supported = self.n_groups == 1 and self.n_bf <= 4
-        g = 0
         for k in range(self.n_eci):
             if self.eci_kind[k] != 2:
                 continue
             t = self.eci_type[k]
-            size = int(self.type_size[t])
-            decos = self.eq_decos[self.eq_off[k]:self.eq_off[k + 1]]
-            n_eq = len(decos)
-            if self.n_groups >= 1 and self.type_m[t, g] > 0:
-                weight[k] = (float(size) / float(n_eq)) / float(int(self.type_M[t]) * int(self.group_count[g]))
-            norm = sum(int(self.type_m[t, s]) * int(self.group_count[s]) for s in range(self.n_groups))
+            n_eq = int(self.eq_off[k + 1] - self.eq_off[k])
+            if int(self.type_M[t]) > 0 and G >= 1:
+                weight[k] = (float(self.type_size[t]) / float(n_eq)) / float(int(self.type_M[t]) * n_ref)
+            norm = sum(int(self.type_m[t, s]) * int(self.group_count[s]) for s in range(G))
             full_weight[k] = 1.0 / (float(n_eq) * float(norm)) if norm else 0.0
-            if self.n_groups < 1:
-                continue
-            off, m = int(self.type_off[t, g]), int(self.type_m[t, g])
-            for deco in decos:
-                for r in range(off, off + m):
-                    order = self.order[r, :size]
-                    inv = np.empty(size, dtype=np.int64)
-                    inv[order] = np.arange(size)
-                    d = [int(deco[inv[p]]) for p in range(size)]
-                    term_eci.append(k)
-                    term_ref.append(d[0])
-                    term_size.append(size)
-                    nb = [int(self.members[r, j]) * self.n_bf + d[j + 1] for j in range(size - 1)]
-                    term_nb.append(nb + [0] * (3 - len(nb)))
+        for g in range(G):
+            pos = {c: j for j, c in enumerate(group_cols[g])}
+            for k in range(self.n_eci):
+                if self.eci_kind[k] != 2:
+                    continue
+                t = self.eci_type[k]
+                size = int(self.type_size[t])
+                decos = self.eq_decos[self.eq_off[k]:self.eq_off[k + 1]]
+                off, m = int(self.type_off[t, g]), int(self.type_m[t, g])
+                for deco in decos:
+                    for r in range(off, off + m):
+                        order = self.order[r, :size]
+                        inv = np.empty(size, dtype=np.int64)
+                        inv[order] = np.arange(size)
+                        d = [int(deco[inv[p]]) for p in range(size)]
+                        term_eci.append(k)
+                        term_ref.append(d[0])
+                        term_size.append(size)
+                        nb = [pos[int(self.members[r, j])] * self.n_bf + d[j + 1] for j in range(size - 1)]
+                        term_nb.append(nb + [0] * (3 - len(nb)))
+            group_terms.append(len(term_eci))
         self.term_eci = np.array(term_eci, dtype=np.int32)
         self.term_ref = np.array(term_ref, dtype=np.int32)
         self.term_size = np.array(term_size, dtype=np.int32)
         self.term_nb = np.array(term_nb if term_nb else np.zeros((0, 3)), dtype=np.int32).reshape(-1, 3)
         self.n_terms = len(term_eci)
+        self.group_terms = np.array(group_terms if G else [0, 0], dtype=np.int32)
         self.eci_weight = weight
         self.eci_full_weight = full_weight
 

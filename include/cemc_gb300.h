@@ -33,6 +33,7 @@ extern "C" {
 #define CEMC_MAX_BF 4         /* decorations per site (species - 1) */
 #define CEMC_MAX_ECI 128      /* ECIs per cluster expansion */
 #define CEMC_MAX_COLS 128     /* distinct neighbour columns per site */
+#define CEMC_MAX_GROUPS 8     /* translation-symmetry groups */
 
 /* Running sums a chain accumulates after every trial (accepted or not).
  * Energies are taken relative to e_ref to keep the squares well conditioned;
@@ -58,7 +59,17 @@ typedef struct {
  *   term_size[t]  cluster size (2..4)
  *   term_nb[t*3+j] packed (column * n_bf + decoration) of member j
  * Terms are sorted by ECI; eci_weight[k] = size / (|eq deco| * M_k * N_s)
- * is the reference's increment normalisation (ce_updater.cpp:400-402). */
+ * is the reference's increment normalisation (ce_updater.cpp:400-402).
+ *
+ * Several translation-symmetry groups (the reference's trans_symm_group,
+ * ce_updater.cpp:733-776): each group has its own terms, which sit in one
+ * contiguous range sorted by ECI (group g owns terms [group_terms[g],
+ * group_terms[g+1])), and its own columns: the table row of a site lists the
+ * neighbours its group's terms name, in the group's column order (unused
+ * trailing columns point at the site itself).  eci_weight holds the
+ * normalisation of group 0; the cluster-ECI change of a site of group g is
+ * multiplied by group_scale[g] = N_0 / N_g (1 when the groups have equal
+ * sizes, as translation classes of a periodic supercell do). */
 typedef struct {
   int32_t n_sites;        /* N, including background sites */
   int32_t n_cols;         /* neighbour columns per site */
@@ -82,6 +93,10 @@ typedef struct {
    * full recompute.  NULL (or n_movable == n_sites) = every site. */
   const int32_t *movable;
   int32_t n_movable;
+  int32_t n_groups;            /* translation-symmetry groups; 0 or 1 = one group (the fields below unused) */
+  const int32_t *site_group;   /* [n_sites] group of each site (background sites: ignored) */
+  const int32_t *group_terms;  /* [n_groups + 1] term range of each group */
+  const double *group_scale;   /* [n_groups] factor on a site's cluster-ECI change, N_0 / N_g */
 } cemc_geometry_desc;
 
 typedef struct cemc_geometry cemc_geometry;

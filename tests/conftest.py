@@ -26,13 +26,23 @@ def load_golden(name):
     return {k: d[k] for k in d.files}
 
 
+def settings_for(lattice, L, ps, ts, qs, syms):
+    """``fcc``, ``l12`` or ``l12:<group of each sublattice>`` settings (the lattice key of a golden case)."""
+    from cemc_gb300.lattice import fcc_settings, l12_settings
+    if lattice.startswith("l12"):
+        gob = tuple(int(ch) for ch in lattice.split(":")[1]) if ":" in lattice else (0, 1, 2, 3)
+        return l12_settings(L, ps, ts, qs, syms, group_of_basis=gob)
+    return fcc_settings(L, ps, ts, qs, syms)
+
+
 def golden_model(g):
     """Rebuild the settings/model of a golden case and check it is the generated one."""
-    from cemc_gb300.lattice import fcc_settings, seeded_ecis, with_background
+    from cemc_gb300.lattice import seeded_ecis, with_background
     from cemc_gb300.tables import CEModel
     ps, ts, qs = (int(x) for x in g["shells"])
     syms = [str(s) for s in g["species"]]
-    s = fcc_settings(int(g["L"]), ps, ts, qs, syms)
+    lattice = str(g["lattice"]) if "lattice" in g else "fcc"
+    s = settings_for(lattice, int(g["L"]), ps, ts, qs, syms)
     bg = str(g["background"]) if "background" in g else ""
     if bg:
         s = with_background(s, bg)

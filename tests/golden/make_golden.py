@@ -35,14 +35,16 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from cemc_gb300.lattice import fcc_settings, seeded_ecis, with_background  # noqa: E402
+from cemc_gb300.lattice import fcc_settings, l12_settings, seeded_ecis, with_background  # noqa: E402
 from cemc_gb300.tables import CEModel  # noqa: E402
 
 KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
 
 # name, L, pair shells, triplet shells, quad shells, species, move (0 flip, 1 swap), T, trials, seed,
 # background symbol (None: every site active; else an inert second sublattice of that species,
-# rocksalt-like, as in the reference's tests/test_sgc_mc.py:140-191)
+# rocksalt-like, as in the reference's tests/test_sgc_mc.py:140-191), lattice ("fcc": one
+# translation-symmetry group; "l12": FCC under L1_2 symmetry, four groups, like the four-group
+# crystal of the reference's tests/helper_functions.py:8-27)
 CASES = [
     ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11, None),
     ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12, None),
@@ -51,6 +53,12 @@ CASES = [
     ("ternary_swap", 4, 5, 3, 1, ["Al", "Mg", "Si"], 1, 800.0, 1500, 15, None),
     ("rocksalt_flip", 4, 4, 2, 1, ["Li", "V"], 0, 800.0, 3000, 16, "O"),
     ("rocksalt_swap", 4, 4, 2, 1, ["Li", "V"], 1, 800.0, 3000, 17, "O"),
+    ("l12_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 18, None, "l12"),
+    ("l12_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 19, None, "l12"),
+    ("l12_ternary_swap", 3, 3, 2, 0, ["Al", "Mg", "Si"], 1, 800.0, 1500, 20, None, "l12"),
+    # corner sublattice + the three face sublattices merged into one group: groups of N/4 and 3N/4 sites
+    ("l12_merged_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 21, None, "l12:0111"),
+    ("l12_merged_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 22, None, "l12:0111"),
 ]
 
 
@@ -62,9 +70,17 @@ def model_hash(m: CEModel) -> str:
     return h.hexdigest()
 
 
-def build_case(name, L, ps, ts, qs, syms, move, T, n, seed, background):
+def make_settings(lattice, L, ps, ts, qs, syms):
+    """``fcc``, ``l12`` or ``l12:<group of each sublattice>`` (e.g. ``l12:0111``)."""
+    if lattice.startswith("l12"):
+        gob = tuple(int(ch) for ch in lattice.split(":")[1]) if ":" in lattice else (0, 1, 2, 3)
+        return l12_settings(L, ps, ts, qs, syms, group_of_basis=gob)
+    return fcc_settings(L, ps, ts, qs, syms)
+
+
+def build_case(name, L, ps, ts, qs, syms, move, T, n, seed, background, lattice="fcc"):
     import oracle as O
-    s = fcc_settings(L, ps, ts, qs, syms)
+    s = make_settings(lattice, L, ps, ts, qs, syms)
     if background:
         s = with_background(s, background)
     eci = seeded_ecis(s.cset, 0)
@@ -130,7 +146,7 @@ def build_case(name, L, ps, ts, qs, syms, move, T, n, seed, background):
 
     return dict(
         L=L, shells=np.array([ps, ts, qs]), species=np.array(syms), move=move, T=T, kT=kT, seed=seed,
-        background=np.array(background or ""),
+        background=np.array(background or ""), lattice=np.array(lattice),
         n_trials=n, model_hash=model_hash(m), eci=ev, eci_names=np.array(m.eci_names),
         occ0=occ0, cf0=cf0, sites=tr.site.reshape(n, 2), u=tr.u, ref_acc=acc, ref_de=de,
         occ_final=occ, cf_final=cf_final, energy_final=cur,

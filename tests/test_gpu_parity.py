@@ -10,7 +10,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import KB, golden_cases, golden_model, load_golden
+from conftest import KB, golden_cases, golden_model, load_golden, settings_for
 
 pytestmark = pytest.mark.gpu
 
@@ -53,12 +53,15 @@ def _run_shape(cb, n, E, **kw):
 
 
 def _kernel_ok(m, kernel, E, move=0, cluster=0):
-    """The spin-basis kernels only take binary +1/-1 geometries; the half-warp one only flips on one CTA."""
+    """The spin-basis kernels only take binary +1/-1 geometries of one translation group; the half-warp one
+    only flips."""
     if kernel in (E.KERNEL_SPIN, E.KERNEL_SPIN_HALFWARP) and not (
-            m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0]):
-        pytest.skip("spin-basis kernel needs a binary +1/-1 basis")
+            m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0] and m.n_groups == 1):
+        pytest.skip("spin-basis kernel needs a binary +1/-1 basis and one translation group")
     if kernel == E.KERNEL_SPIN_HALFWARP and move != 0:
         pytest.skip("the half-warp spin kernel runs flips")
+    if kernel == E.KERNEL_TABLE and np.any(np.asarray(m.group_scale) != 1.0):
+        pytest.skip("the table kernel needs translation groups of equal size")
 
 
 KERNELS = [1, 2, 3, 4]  # generic, spin, spin half-warp, table
@@ -155,12 +158,14 @@ def test_gpu_delta_e_matches_oracle(E, oracle_mod):
         assert np.allclose(dcf, c2 - g["cf0"], atol=1e-13)
 
 
-@pytest.mark.parametrize("recipe", [(6, 4, 2, 1, ["Al", "Mg"]), (4, 5, 3, 1, ["Al", "Mg", "Si"])])
+@pytest.mark.parametrize("recipe", [(6, 4, 2, 1, ["Al", "Mg"], "fcc"), (4, 5, 3, 1, ["Al", "Mg", "Si"], "fcc"),
+                                    (4, 4, 2, 1, ["Al", "Mg"], "l12"), (3, 3, 2, 0, ["Al", "Mg", "Si"], "l12"),
+                                    (4, 4, 2, 1, ["Al", "Mg"], "l12:0111")])
 def test_gpu_full_recompute_matches_oracle(recipe, E, oracle_mod):
-    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.lattice import seeded_ecis
     from cemc_gb300.tables import CEModel
-    L, ps, ts, qs, syms = recipe
-    s = fcc_settings(L, ps, ts, qs, syms)
+    L, ps, ts, qs, syms, lattice = recipe
+    s = settings_for(lattice, L, ps, ts, qs, syms)
     eci = seeded_ecis(s.cset, 2)
     m = CEModel(s, list(eci))
     orc = oracle_mod.Oracle(m)
@@ -300,6 +305,89 @@ def test_gpu_replica_exchange_matches_restatement(E):
             assert np.array_equal(rep_d.cpu().numpy(), rep)
             assert np.array_equal(kT_d.cpu().numpy(), kT)
             assert int(nacc.item()) == acc
+
+
+@pytest.mark.parametrize("case", ["l12_swap", "l12_merged_swap", "l12_ternary_swap"])
+@pytest.mark.parametrize("kernel", [1, 4])
+@pytest.mark.parametrize("move", [0, 1])
+def test_gpu_multi_group_batch_equals_oracle(case, kernel, move, E, oracle_mod):
+    """Several translation groups: chains with their own keys, temperatures and occupations, flips
+    and swaps (within and across groups), each equal to the oracle's run of that chain."""
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    assert m.n_groups > 1
+    _kernel_ok(m, kernel, E, move)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(17)
+    n_chains = 4
+    occ = rng.integers(0, m.n_sym, (n_chains, m.n_sites)).astype(np.int8)
+    Ts = np.linspace(400, 1600, n_chains)
+    ev = np.repeat(g["eci"][None], n_chains, 0)
+    keys = [3, 9, 4, 21]
+    cb = E.ChainBatch(geo, occ, ev, KB * Ts, move, seed=5, chain_keys=keys)
+    n = 2000
+    _, acc, de = cb.run(n, precision=E.PREC_F64, warps=12, trace=True, kernel=kernel)
+    _sync()
+    cb.check_status()
+    assert cb.last_kernel == kernel
+    acc = acc.cpu().numpy()
+    de = de.cpu().numpy()
+    for c in range(n_chains):
+        st = orc.new_chain_state(occ[c], ev[c], KB * Ts[c], move)
+        tr = orc.run(st, seed=5, chain_id=keys[c], t_begin=0, n_trials=n, trace=True)
+        assert np.array_equal(acc[c], tr.acc)
+        assert np.max(np.abs(de[c] - tr.de)) < 1e-9
+        assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
+        assert _cf_close(cb.cf.cpu().numpy()[c], st.cf)
+
+
+def test_gpu_multi_group_kernel_selection(E):
+    """Four equal groups run the table form by default; unequal groups the generic form, and neither
+    takes the spin form."""
+    from cemc_gb300._lib import CemcError
+    for case, auto_kernel in (("l12_swap", E.KERNEL_TABLE), ("l12_merged_swap", E.KERNEL_GENERIC)):
+        g = load_golden(case)
+        s, m, eci = golden_model(g)
+        geo = E.Geometry(m)
+        cb = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), 1, seed=1)
+        cb.run(100)
+        _sync()
+        assert cb.last_kernel == auto_kernel
+        with pytest.raises(CemcError) as ei:
+            cb.run(10, kernel=E.KERNEL_SPIN)
+        assert ei.value.code == 1
+        if auto_kernel == E.KERNEL_GENERIC:
+            with pytest.raises(CemcError) as ei:
+                cb.run(10, kernel=E.KERNEL_TABLE)
+            assert ei.value.code == 5
+
+
+def test_gpu_multi_group_delta_e_matches_oracle(E, oracle_mod):
+    """The calculator's energy change of swaps between sites of different translation groups."""
+    g = load_golden("l12_ternary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    from cemc_gb300.calculator import DeviceUpdater
+    up = DeviceUpdater(geo, g["occ0"], g["eci"], cf=g["cf0"])
+    occ = g["occ0"].copy()
+    rng = np.random.default_rng(3)
+    e0 = orc.energy(g["eci"], g["cf0"])
+    n_cross = 0
+    for _ in range(40):
+        a, b = (int(x) for x in rng.choice(m.n_sites, 2, replace=False))
+        if occ[a] == occ[b]:
+            continue
+        n_cross += int(m.site_group[a] != m.site_group[b])
+        de, dcf = up.delta_swap(a, b)
+        c1 = orc.update_cf(occ, a, occ[b], g["cf0"])
+        o2 = occ.copy()
+        o2[a] = occ[b]
+        c2 = orc.update_cf(o2, b, occ[a], c1)
+        assert abs(de - (orc.energy(g["eci"], c2) - e0)) < 1e-9
+        assert np.allclose(dcf, c2 - g["cf0"], atol=1e-13)
+    assert n_cross > 5
 
 
 def test_gpu_spin_kernel_rejects_ternary(E):
