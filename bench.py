@@ -400,7 +400,7 @@ def run_canonical1(args):
     cb = E.ChainBatch(geo, occ[None], ev, KB * 800.0, E.MOVE_SWAP, seed=0)
     n = m.n_sites * 1000
     stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
-    t, clocks = _timed_steps(lambda: cb.run(n, precision=E.PREC_F64, warps=args.warps or 16), stream, args.steps,
+    t, clocks = _timed_steps(lambda: cb.run(n, precision=E.PREC_F64, warps=args.warps or 0), stream, args.steps,
                              args.warmup, local)
     cb.check_status()
     cpu = None
@@ -420,7 +420,8 @@ def run_canonical1(args):
                           "warmup": args.warmup, "dtype": "f64", "clocks": clocks, "cpu_baseline": cpu,
                           "accept_rate": float(cb.accum_host()[0, E.A_NACC] / max(cb.accum_host()[0, E.A_NSAMP], 1)),
                           "config": {"workload": "canonical_swap_fcc_binary_8x8x8_1chain", "n_sites": m.n_sites,
-                                     "trials_per_step": n, "T": 800.0, "precision": "fp64"}}))
+                                     "trials_per_step": n, "T": 800.0, "precision": "fp64",
+                                     "kernel": int(cb.last_kernel), "warps_per_cta": args.warps or "auto"}}))
     return 0
 
 

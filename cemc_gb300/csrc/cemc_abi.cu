@@ -540,7 +540,19 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   // (a CTA pair takes the half-warp form only when that form is asked for explicitly)
   const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
                                                                 r->cluster != 2)) ? 2 : 1;
-  int warps = r->warps > 0 ? r->warps : 16;
+  // Default round width: 16 evaluating warps, fewer where most trials of a
+  // round would conflict.  A changed site reaches about n_cols sites, so with
+  // n_movable / (2 n_cols sites-per-move) trials a round about half the round
+  // commits (a 2048-site swap chain: 9 trials, about 4 commits a round); a
+  // wider round only adds latency.  The same cap decides whether a chain may
+  // take a CTA pair (twice the trials per round) when none is asked for.
+  int warps = r->warps;
+  int round_cap = 0;  // 0: the caller chose the width
+  if (warps <= 0) {
+    const int per_move = r->move == CEMC_MOVE_SWAP ? 2 : 1;
+    round_cap = std::max(4, g.n_movable / (2 * g.n_cols * per_move));
+    warps = std::max(2, std::min(16, round_cap / tpw));
+  }
   const int rsize = r->precision == CEMC_PREC_F32 ? 4 : 8;
   cemc::RunArgs a{};
   a.n_chains = r->n_chains;
@@ -630,7 +642,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   bool found = false;
   for (size_t fi = 0; fi < forms.size() && !found; ++fi) {
     form = forms[fi];
-    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && 2 * r->n_chains <= geo->n_sms)) {
+    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && 2 * r->n_chains <= geo->n_sms &&
+                            (round_cap == 0 || round_cap >= 2 * warps))) {
       cemc::RunArgs x = a;
       cemc::McLayout L2{};
       if (fit(2, L2, x)) {

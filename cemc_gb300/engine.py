@@ -238,6 +238,57 @@ class ChainBatch:
     def set_temperature(self, kT):
         self.kT.copy_(torch.as_tensor(np.broadcast_to(np.asarray(kT, dtype=np.float64), (self.n_chains,)).copy()))
 
+    # -- checkpoint ------------------------------------------------------------
+    _STATE = ("occ", "cf", "energy", "eci", "kT", "trial", "accum", "chain_key", "trk", "loc", "trk_start",
+              "trk_count")
+
+    def state_dict(self) -> dict:
+        """Host copy of everything a continued run reads, bit for bit.
+
+        Occupations, correlation functions, energies, ECIs, temperatures, the
+        trial counter of each chain's counter-based stream, the running sums
+        (their two uint64 counters kept as raw bits) and, for swaps, the
+        per-species site lists, whose order decides which site a later trial
+        draws.  A batch restored from it continues exactly as this one would.
+        """
+        torch.cuda.synchronize(self.occ.device)
+        out = {"move": np.array(self.move), "seed": np.array(self.seed, dtype=np.uint64),
+               "n_sites": np.array(self.geo.model.n_sites), "n_eci": np.array(self.geo.model.n_eci)}
+        for name in self._STATE:
+            t = getattr(self, name, None)
+            if t is not None:
+                out[name] = t.cpu().numpy().copy()
+        return out
+
+    def load_state_dict(self, st: dict):
+        """Restore ``state_dict`` output into this batch (same geometry, chain count and move)."""
+        m = self.geo.model
+        if int(st["move"]) != self.move or int(st["n_sites"]) != m.n_sites or int(st["n_eci"]) != m.n_eci:
+            raise ValueError("checkpoint is of another move type or geometry")
+        if np.asarray(st["occ"]).reshape(-1, m.n_sites).shape[0] != self.n_chains:
+            raise ValueError("checkpoint holds %d chains, this batch %d"
+                             % (np.asarray(st["occ"]).reshape(-1, m.n_sites).shape[0], self.n_chains))
+        self.seed = int(np.asarray(st["seed"]).astype(np.uint64))
+        dev = self.occ.device
+        for name in self._STATE:
+            t = getattr(self, name, None)
+            if name not in st:
+                continue
+            src = torch.as_tensor(np.ascontiguousarray(st[name]))
+            if t is None:
+                setattr(self, name, src.to(dev))
+            else:
+                t.copy_(src.view(t.shape).to(dev, dtype=t.dtype))
+        torch.cuda.synchronize(dev)
+
+    def save(self, fname):
+        """``state_dict`` as a NumPy ``.npz`` file (no pickled objects)."""
+        np.savez(fname, **self.state_dict())
+
+    def load(self, fname):
+        with np.load(fname, allow_pickle=False) as d:
+            self.load_state_dict({k: d[k] for k in d.files})
+
     # -- library calls -----------------------------------------------------
     def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
             chain_trials: Optional[torch.Tensor] = None, kernel: int = 0, cluster: int = 0):

@@ -398,6 +398,67 @@ class Montecarlo:
             obs([])
         return totalenergies
 
+    # -- checkpoint / restart (montecarlo.py:1040-1074) ---------------------------------
+    _CHECKPOINT_ATTRS = ("T", "min_acc_rate", "current_step", "num_accepted", "status_every_sec", "energy_bias",
+                         "correlation_info", "precision", "warps", "recompute_every_sweeps", "seed", "symbols",
+                         "current_energy", "logfile", "name")
+
+    def _checkpoint_attrs(self):
+        return self._CHECKPOINT_ATTRS
+
+    def save(self, fname):
+        """Store the run so that ``load`` continues it exactly where it stopped.
+
+        The reference pickles the whole driver with dill (montecarlo.py:1040-1056).
+        Here the file (a pickle of plain data) holds the driver's attributes, the
+        calculator's settings object, ECIs and symbols, and the chain's device state
+        (``ChainBatch.state_dict``: occupation, correlation functions, energy, the
+        trial counter of the counter-based stream, the running sums and the swap
+        site lists), so a loaded driver draws the same trials and reaches
+        bit-identical states.  Observers are not stored: like the reference does
+        for observers it cannot serialise, the caller attaches them again.
+        """
+        import pickle
+        calc = self._calc()
+        state = {"format": "cemc_gb300.montecarlo/1", "class": type(self).__name__,
+                 "attrs": {k: getattr(self, k) for k in self._checkpoint_attrs()},
+                 "settings": calc.BC, "eci": dict(calc.eci), "symbols": [a.symbol for a in self.atoms],
+                 "chain": self.chain().state_dict()}
+        with open(fname, "wb") as f:
+            pickle.dump(state, f, protocol=4)
+
+    @staticmethod
+    def load(fname, atoms=None, device="cuda"):
+        """Rebuild a driver saved by ``save`` (montecarlo.py:1058-1074).
+
+        ``atoms``: container to attach the calculator to (its symbols are set
+        from the file); default a ``SimpleAtoms`` of the saved symbols.
+        """
+        import pickle
+        from .calculator import CE, SimpleAtoms
+        with open(fname, "rb") as f:
+            state = pickle.load(f)
+        if state.get("format") != "cemc_gb300.montecarlo/1":
+            raise ValueError("%s is not a Monte Carlo checkpoint of this library" % fname)
+        klass = {"Montecarlo": Montecarlo, "SGCMonteCarlo": SGCMonteCarlo}[state["class"]]
+        if atoms is None:
+            atoms = SimpleAtoms(state["symbols"])
+        else:
+            for a, sym in zip(atoms, state["symbols"]):
+                a.symbol = sym
+        ch_state = state["chain"]
+        names = sorted(state["eci"])  # the calculator keeps its correlation functions in sorted-name order
+        CE(atoms, state["settings"], eci=dict(state["eci"]),
+           initial_cf=dict(zip(names, np.asarray(ch_state["cf"], dtype=np.float64).reshape(-1).tolist())),
+           device=device)
+        a = state["attrs"]
+        mc = klass(atoms, a["T"], seed=a["seed"], precision=a["precision"], warps=a["warps"],
+                   recompute_every_sweeps=a["recompute_every_sweeps"])
+        for k, v in a.items():
+            setattr(mc, k, v)
+        mc.chain().load_state_dict(ch_state)
+        return mc
+
     @property
     def meta_info(self):
         import datetime
@@ -450,6 +511,9 @@ class SGCMonteCarlo(Montecarlo):
 
     def _check_symbols(self):
         pass
+
+    _CHECKPOINT_ATTRS = Montecarlo._CHECKPOINT_ATTRS + ("chem_pots", "chem_pot_names", "chem_pot_in_ecis",
+                                                        "_chemical_potential")
 
     @property
     def chemical_potential(self):

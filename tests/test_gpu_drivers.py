@@ -292,3 +292,65 @@ def test_table_form_leaves_exact_correlation_functions(torch_cuda, oracle_mod):
             assert np.allclose(cb.cf.cpu().numpy()[c], full, rtol=1e-12, atol=1e-15)
             assert abs(cb.energy.cpu().numpy()[c] - orc.energy(m.eci_vector(eci), full)) < 1e-9 * abs(
                 orc.energy(m.eci_vector(eci), full))
+
+
+@pytest.mark.parametrize("driver", ["canonical", "sgc"])
+def test_montecarlo_checkpoint_resume_is_exact(driver, torch_cuda, tmp_path):
+    """A driver saved mid-run and loaded again continues bit for bit like one that never stopped
+    (Montecarlo.save / load, montecarlo.py:1040-1074)."""
+    torch = torch_cuda
+    from cemc_gb300.mcmc import Montecarlo, SGCMonteCarlo
+
+    def make():
+        atoms, calc, s, eci = _calc(recipe=(4, 4, 2, 1, ("Al", "Mg")), seed=2)
+        if driver == "sgc":
+            mc = SGCMonteCarlo(atoms, 900.0, seed=21)
+            mc.chemical_potential = {"c1_0": 0.05}
+        else:
+            mc = Montecarlo(atoms, 700.0, seed=21)
+        return mc
+
+    a = make()
+    a._run_trials(7000)
+    path = str(tmp_path / "mc.ckpt")
+    a.save(path)
+    a._run_trials(9000)
+    b = Montecarlo.load(path)
+    assert type(b) is type(a) and b.current_step == 7000
+    b._run_trials(9000)
+    ca, cb = a.chain(), b.chain()
+    for name in ("occ", "cf", "energy", "trial", "accum", "eci", "kT"):
+        assert torch.equal(getattr(ca, name), getattr(cb, name)), name
+    if driver == "canonical":
+        assert torch.equal(ca.trk, cb.trk) and torch.equal(ca.loc, cb.loc)
+    assert [x.symbol for x in a.atoms] == [x.symbol for x in b.atoms]
+    qa, qb = a.get_thermodynamic(), b.get_thermodynamic()
+    for k, v in qa.items():
+        if k != "timestamp":
+            assert qb[k] == v, k
+
+
+@pytest.mark.parametrize("move", [0, 1])
+def test_chain_batch_checkpoint_resume_is_exact(move, torch_cuda, tmp_path):
+    """ChainBatch.save / load: a batch restored from a checkpoint continues identically."""
+    torch = torch_cuda
+    from cemc_gb300 import engine as E
+    g = load_golden("ternary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(3)
+    occ = rng.integers(0, m.n_sym, (5, m.n_sites)).astype(np.int8)
+    kT = KB * np.linspace(500, 1500, 5)
+    a = E.ChainBatch(geo, occ, g["eci"], kT, move, seed=77, chain_keys=[4, 1, 9, 2, 6])
+    a.run(3000, warps=8)
+    path = str(tmp_path / "batch.npz")
+    a.save(path)
+    a.run(4000, warps=8)
+    b = E.ChainBatch(geo, occ, g["eci"], KB * 300.0, move, seed=1)
+    b.load(path)
+    b.run(4000, warps=8)
+    torch.cuda.synchronize()
+    for name in ("occ", "cf", "energy", "trial", "accum", "kT", "chain_key"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    with pytest.raises(ValueError):
+        E.ChainBatch(geo, occ[:2], g["eci"], kT[:2], move, seed=1).load(path)
