@@ -1,13 +1,14 @@
-"""FCC supercells, cluster enumeration and the settings object a CE updater reads.
+"""Cubic supercells, cluster enumeration and the settings object a CE updater reads.
 
 The reference takes its lattice, clusters, translation matrix and basis
 functions from a CLEASE settings object (``BC``) and parses it in
 ``cpp/src/ce_updater.cpp:43-212`` and ``cpp/src/cluster.cpp:185-232``.  CLEASE is
 not part of this project, so this module generates the same information for
-face-centred-cubic supercells from the geometry alone:
+cubic supercells (FCC, BCC, SC; and FCC with the four sublattices of its L1_2
+ordering as separate translation-symmetry groups) from the geometry alone:
 
-* sites of an ``L x L x L`` conventional cubic supercell (4 sites per cube),
-  ordered like ``bulk(..., cubic=True).repeat((L, L, L))``;
+* sites of an ``L x L x L`` conventional cubic supercell (4, 2 or 1 sites per
+  cube), ordered like ``bulk(..., cubic=True).repeat((L, L, L))``;
 * neighbour shells and all pair / triplet / quadruplet clusters that contain
   the reference site 0, classified into symmetry-distinct types with the 48
   operations of the cubic point group plus lattice translations;
@@ -34,9 +35,25 @@ from typing import Dict, List, Sequence, Tuple
 
 import numpy as np
 
-# Conventional FCC basis in half-lattice-constant units.
+# Conventional cubic bases in half-lattice-constant units (site order inside a cube).
 _FCC_BASIS = np.array([(0, 0, 0), (0, 1, 1), (1, 0, 1), (1, 1, 0)], dtype=np.int64)
-_BASIS_INDEX = {(0, 0, 0): 0, (0, 1, 1): 1, (1, 0, 1): 2, (1, 1, 0): 3}
+_CUBIC_BASES = {
+    "fcc": _FCC_BASIS,
+    "bcc": np.array([(0, 0, 0), (1, 1, 1)], dtype=np.int64),
+    "sc": np.array([(0, 0, 0)], dtype=np.int64),
+}
+
+
+def _is_lattice_vector(kind: str, g: np.ndarray) -> np.ndarray:
+    """Rows of ``g`` (half-lattice units) that are vectors of the cubic Bravais lattice ``kind``."""
+    if kind == "fcc":
+        return g.sum(axis=1) % 2 == 0
+    if kind == "bcc":
+        par = np.mod(g, 2)
+        return (par == par[:, :1]).all(axis=1)
+    if kind == "sc":
+        return (np.mod(g, 2) == 0).all(axis=1)
+    raise ValueError("unknown lattice %r (fcc, bcc or sc)" % kind)
 
 
 def _cubic_point_group() -> np.ndarray:
@@ -54,18 +71,19 @@ def _cubic_point_group() -> np.ndarray:
 _OH = _cubic_point_group()
 
 
-def fcc_shell_vectors(max_shell: int) -> List[np.ndarray]:
-    """Neighbour vectors of the FCC lattice (half-lattice units), one array per shell.
+def shell_vectors(kind: str, max_shell: int) -> List[np.ndarray]:
+    """Neighbour vectors of a cubic Bravais lattice (half-lattice units), one array per shell.
 
     Shell k (1-based) holds every lattice vector with the k-th smallest
     non-zero length.  FCC lattice vectors are the integer vectors whose
-    coordinate sum is even.
+    coordinate sum is even; BCC ones have coordinates of one parity; SC ones
+    are even.
     """
     r = 2
     while True:
         rng = np.arange(-r, r + 1)
         g = np.array(np.meshgrid(rng, rng, rng, indexing="ij")).reshape(3, -1).T
-        g = g[(g.sum(axis=1) % 2 == 0) & (np.abs(g).sum(axis=1) > 0)]
+        g = g[_is_lattice_vector(kind, g) & (np.abs(g).sum(axis=1) > 0)]
         d2 = (g * g).sum(axis=1)
         radii = np.unique(d2)
         # Every shell up to max_shell is complete if its radius is below r^2.
@@ -79,8 +97,12 @@ def fcc_shell_vectors(max_shell: int) -> List[np.ndarray]:
         r += 1
 
 
-def shell_radius2(max_shell: int) -> List[int]:
-    return [int((s[0] * s[0]).sum()) for s in fcc_shell_vectors(max_shell)]
+def fcc_shell_vectors(max_shell: int) -> List[np.ndarray]:
+    return shell_vectors("fcc", max_shell)
+
+
+def shell_radius2(max_shell: int, kind: str = "fcc") -> List[int]:
+    return [int((s[0] * s[0]).sum()) for s in shell_vectors(kind, max_shell)]
 
 
 @dataclass
@@ -163,15 +185,16 @@ def _equiv_sites(proto: np.ndarray) -> List[List[int]]:
     return [sorted(gq) for gq in sorted(groups.values()) if len(gq) >= 2]
 
 
-def enumerate_cluster_types(pair_shells: int, triplet_shells: int, quad_shells: int) -> List[ClusterType]:
-    """All pair/triplet/quad types of the FCC lattice with max distance in the given shells.
+def enumerate_cluster_types(pair_shells: int, triplet_shells: int, quad_shells: int,
+                            kind: str = "fcc") -> List[ClusterType]:
+    """All pair/triplet/quad types of a cubic Bravais lattice with max distance in the given shells.
 
     A cluster of size >= 3 belongs to the set if every pairwise distance is at
     most the radius of shell ``triplet_shells`` (resp. ``quad_shells``); size 0
-    means "no clusters of that size".
+    means "no clusters of that size".  Symmetry: lattice translations and O_h.
     """
     max_shell = max(pair_shells, triplet_shells, quad_shells, 1)
-    shells = fcc_shell_vectors(max_shell)
+    shells = shell_vectors(kind, max_shell)
     radii = [int((s[0] * s[0]).sum()) for s in shells]
     types: List[ClusterType] = []
 
@@ -254,34 +277,51 @@ def ternary_basis(symbols: Sequence[str]) -> List[Dict[str, float]]:
     return [phi1, phi2]
 
 
-class FCCSupercell:
-    """Sites and periodic translation of an ``L x L x L`` conventional FCC supercell."""
+class CubicSupercell:
+    """Sites and periodic translation of an ``L x L x L`` supercell of conventional cubes.
 
-    def __init__(self, L: int, a: float = 4.05):
+    ``kind`` is ``fcc`` (4 sites per cube), ``bcc`` (2) or ``sc`` (1); sites
+    are ordered cube by cube, basis order inside a cube, like
+    ``bulk(..., cubic=True).repeat((L, L, L))``.
+    """
+
+    def __init__(self, L: int, a: float = 4.05, kind: str = "fcc"):
         if L < 1:
             raise ValueError("supercell size must be positive")
+        if kind not in _CUBIC_BASES:
+            raise ValueError("unknown lattice %r (fcc, bcc or sc)" % kind)
+        self.kind = kind
+        self.basis = _CUBIC_BASES[kind]
         self.L = int(L)
         self.a = float(a)
         self.period = 2 * self.L
         cells = np.array(list(itertools.product(range(L), repeat=3)), dtype=np.int64)
-        pos = (2 * cells)[:, None, :] + _FCC_BASIS[None, :, :]
+        pos = (2 * cells)[:, None, :] + self.basis[None, :, :]
         self.positions = pos.reshape(-1, 3)  # half-lattice units
         self.n_sites = len(self.positions)
+        self._parity_code = {tuple(b.tolist()): i for i, b in enumerate(self.basis)}
 
     def index_of(self, pos: np.ndarray) -> np.ndarray:
         """Site index of (possibly unwrapped) positions, shape (..., 3)."""
         p = np.mod(pos, self.period)
         cell = p // 2
         parity = p % 2
-        b = np.zeros(p.shape[:-1], dtype=np.int64)
-        b[(parity == (0, 1, 1)).all(-1)] = 1
-        b[(parity == (1, 0, 1)).all(-1)] = 2
-        b[(parity == (1, 1, 0)).all(-1)] = 3
-        valid = ((parity == (0, 0, 0)).all(-1) | (b > 0))
-        if not np.all(valid):
-            raise ValueError("position is not an FCC lattice site")
+        code = (parity[..., 0] * 4 + parity[..., 1] * 2 + parity[..., 2]).astype(np.int64)
+        lut = np.full(8, -1, dtype=np.int64)
+        for par, i in self._parity_code.items():
+            lut[par[0] * 4 + par[1] * 2 + par[2]] = i
+        b = lut[code]
+        if np.any(b < 0):
+            raise ValueError("position is not a %s lattice site" % self.kind.upper())
         L = self.L
-        return ((cell[..., 0] * L + cell[..., 1]) * L + cell[..., 2]) * 4 + b
+        return ((cell[..., 0] * L + cell[..., 1]) * L + cell[..., 2]) * len(self.basis) + b
+
+
+class FCCSupercell(CubicSupercell):
+    """``L x L x L`` conventional FCC supercell (4 sites per cube)."""
+
+    def __init__(self, L: int, a: float = 4.05):
+        super().__init__(L, a, "fcc")
 
 
 @dataclass
@@ -329,8 +369,9 @@ class ClusterSet:
         return np.array(sorted(offs), dtype=np.int64).reshape(-1, 3)
 
 
-def fcc_cluster_set(pair_shells: int, triplet_shells: int, quad_shells: int, n_species: int) -> ClusterSet:
-    return ClusterSet(enumerate_cluster_types(pair_shells, triplet_shells, quad_shells), n_species - 1)
+def fcc_cluster_set(pair_shells: int, triplet_shells: int, quad_shells: int, n_species: int,
+                    kind: str = "fcc") -> ClusterSet:
+    return ClusterSet(enumerate_cluster_types(pair_shells, triplet_shells, quad_shells, kind), n_species - 1)
 
 
 class Settings:
@@ -344,7 +385,7 @@ class Settings:
     It also carries the packed arrays the GPU path uses.
     """
 
-    def __init__(self, cell: FCCSupercell, cset: ClusterSet, symbols: Sequence[str]):
+    def __init__(self, cell: CubicSupercell, cset: ClusterSet, symbols: Sequence[str]):
         self.cell = cell
         self.cset = cset
         self.unique_elements = sorted(symbols)
@@ -382,7 +423,7 @@ class Settings:
                 "max_cluster_dia": 0.5 * cell.a * math.sqrt(t.dia2),
                 "symm_group": 0,
                 "name": t.name,
-                "descriptor": "fcc_%d_body_d2_%d" % (t.size, t.dia2),
+                "descriptor": "%s_%d_body_d2_%d" % (cell.kind, t.size, t.dia2),
                 "indices": indices,
                 "order": [list(o) for o in t.order],
                 "equiv_sites": [list(g) for g in t.equiv_sites],
@@ -463,6 +504,17 @@ def fcc_settings(L: int, pair_shells: int, triplet_shells: int, quad_shells: int
                  symbols: Sequence[str], a: float = 4.05) -> Settings:
     cset = fcc_cluster_set(pair_shells, triplet_shells, quad_shells, len(symbols))
     return Settings(FCCSupercell(L, a), cset, symbols)
+
+
+def cubic_settings(kind: str, L: int, pair_shells: int, triplet_shells: int, quad_shells: int,
+                   symbols: Sequence[str], a: float = 4.05) -> Settings:
+    """Settings of an ``L^3``-cube supercell of the cubic Bravais lattice ``kind`` (fcc, bcc, sc).
+
+    The reference's tests build BCC and SC cells through CLEASE
+    (tests/test_CE_updater.py:21, 206-228); one translation-symmetry group.
+    """
+    cset = fcc_cluster_set(pair_shells, triplet_shells, quad_shells, len(symbols), kind)
+    return Settings(CubicSupercell(L, a, kind), cset, symbols)
 
 
 def seeded_ecis(cset: ClusterSet, seed: int, c0: float = -3.0, singlet_sigma: float = 0.05,

@@ -35,7 +35,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from cemc_gb300.lattice import fcc_settings, l12_settings, seeded_ecis, with_background  # noqa: E402
+from cemc_gb300.lattice import cubic_settings, fcc_settings, l12_settings, seeded_ecis, with_background  # noqa: E402
 from cemc_gb300.tables import CEModel  # noqa: E402
 
 KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
@@ -44,7 +44,7 @@ KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
 # background symbol (None: every site active; else an inert second sublattice of that species,
 # rocksalt-like, as in the reference's tests/test_sgc_mc.py:140-191), lattice ("fcc": one
 # translation-symmetry group; "l12": FCC under L1_2 symmetry, four groups, like the four-group
-# crystal of the reference's tests/helper_functions.py:8-27)
+# crystal of the reference's tests/helper_functions.py:8-27; "bcc", "sc": other cubic lattices)
 CASES = [
     ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11, None),
     ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12, None),
@@ -59,6 +59,9 @@ CASES = [
     # corner sublattice + the three face sublattices merged into one group: groups of N/4 and 3N/4 sites
     ("l12_merged_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 21, None, "l12:0111"),
     ("l12_merged_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 22, None, "l12:0111"),
+    # other cubic Bravais lattices (the reference's tests use BCC and SC cells, test_CE_updater.py:21,206-228)
+    ("bcc_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 23, None, "bcc"),
+    ("sc_ternary_flip", 5, 3, 2, 1, ["Al", "Mg", "Si"], 0, 800.0, 1500, 24, None, "sc"),
 ]
 
 
@@ -75,6 +78,8 @@ def make_settings(lattice, L, ps, ts, qs, syms):
     if lattice.startswith("l12"):
         gob = tuple(int(ch) for ch in lattice.split(":")[1]) if ":" in lattice else (0, 1, 2, 3)
         return l12_settings(L, ps, ts, qs, syms, group_of_basis=gob)
+    if lattice in ("bcc", "sc"):
+        return cubic_settings(lattice, L, ps, ts, qs, syms)
     return fcc_settings(L, ps, ts, qs, syms)
 
 

@@ -149,3 +149,39 @@ def test_model_rejects_unknown_eci():
     s = fcc_settings(4, 4, 2, 1, ["Al", "Mg"])
     with pytest.raises(ValueError):
         CEModel(s, ["c0", "c1_0", "c7_d9999_0_0000000"])
+
+
+def test_cubic_lattice_shells_and_neighbour_symmetry():
+    """BCC / SC shells (8, 6, 12, 24 and 6, 12, 8, 6 neighbours) and a symmetric neighbour relation."""
+    from cemc_gb300.lattice import cubic_settings, shell_vectors
+    assert [len(v) for v in shell_vectors("bcc", 4)] == [8, 6, 12, 24]
+    assert [len(v) for v in shell_vectors("sc", 4)] == [6, 12, 8, 6]
+    for kind, L in (("bcc", 4), ("sc", 5)):
+        s = cubic_settings(kind, L, 3, 2, 0, ["Al", "Mg"])
+        tab = s.table
+        rows = [set(r.tolist()) for r in tab]
+        for i in range(s.n_sites):
+            for j in rows[i]:
+                assert i in rows[j]
+        m = CEModel(s, list(seeded_ecis(s.cset, 0)))
+        assert m.n_groups == 1 and np.array_equal(m.gpu_table, m.table)
+
+
+def test_l12_groups_share_names_and_pack_columns():
+    """Four translation groups of equal size; the three face groups see the same cluster names; each
+    group's table row lists only its own neighbours (self-padded), and the relation stays symmetric."""
+    from cemc_gb300.lattice import l12_settings
+    s = l12_settings(4, 4, 2, 1, ["Al", "Mg"])
+    assert [len(g) for g in s.index_by_trans_symm] == [64, 64, 64, 64]
+    names = [set(d) for d in s.cluster_info]
+    assert names[1] == names[2] == names[3] and names[0] != names[1]
+    m = CEModel(s, list(seeded_ecis(s.cset, 0)))
+    assert m.n_groups == 4 and m.gpu_n_cols == 54 and m.n_cols > 54
+    assert np.allclose(m.group_scale, 1.0)
+    rows = [set(r.tolist()) for r in m.gpu_table]
+    for i in range(m.n_sites):
+        for j in rows[i]:
+            assert i in rows[j]
+    merged = CEModel(l12_settings(4, 4, 2, 1, ["Al", "Mg"], group_of_basis=(0, 1, 1, 1)),
+                     list(seeded_ecis(s.cset, 0)))
+    assert merged.n_groups == 2 and np.allclose(merged.group_scale, [1.0, 1.0 / 3.0])
