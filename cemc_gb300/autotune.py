@@ -83,6 +83,7 @@ def tune_on(cb, precision: int, shapes=None, sweeps: float = 0.25) -> Dict[tuple
     """Trials/s of each shape on the caller's own batch; its state is restored afterwards."""
     shapes = list(shapes) if shapes is not None else candidates(cb.geo, cb.n_chains)
     names = ["occ", "cf", "energy", "trial", "accum"] + (["trk", "loc"] if cb.trk is not None else [])
+    torch.cuda.synchronize()  # the batch's own stream may still be writing its state
     snap = {n: getattr(cb, n).clone() for n in names}
     trials = max(256, int(sweeps * cb.geo.n_sites))
     stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()

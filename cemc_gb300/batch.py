@@ -60,7 +60,8 @@ class BatchRunner:
         """Capture one step (MC launch + drift-reset recompute) as a CUDA graph."""
         if not self.use_graph or self._graph is not None:
             return
-        # warm the launch path (shared-memory attributes, lazy loading) outside the capture
+        # warm the launch path (shared-memory attributes, lazy loading) outside the capture; the
+        # snapshot, the warm step and the restore are ordered on the runner's stream
         snapshot = self.snapshot()
         with torch.cuda.stream(self.stream):
             self._step_body(self.recompute_every == 1)
@@ -90,15 +91,20 @@ class BatchRunner:
 
     # -- state transfer (the served / end-to-end path) -------------------------------
     def snapshot(self) -> Dict[str, torch.Tensor]:
+        """Copies of the chain state, taken in order on the runner's stream (after its queued work)."""
         cb = self.cb
         names = ["occ", "cf", "energy", "eci", "kT", "trial", "accum"]
         if cb.trk is not None:
             names += ["trk", "loc"]
-        return {n: getattr(cb, n).clone() for n in names}
+        with torch.cuda.stream(self.stream):
+            return {n: getattr(cb, n).clone() for n in names}
 
     def restore(self, snap: Dict[str, torch.Tensor]):
-        for n, t in snap.items():
-            getattr(self.cb, n).copy_(t)
+        """Write a snapshot back, in order on the runner's stream: a launch still running there
+        (the stream's own work) finishes before the state is overwritten."""
+        with torch.cuda.stream(self.stream):
+            for n, t in snap.items():
+                getattr(self.cb, n).copy_(t)
 
     def load_state(self, occ: torch.Tensor, eci: Optional[torch.Tensor] = None, kT: Optional[torch.Tensor] = None):
         """Copy new configurations (host or device tensors) into the resident state and rebuild derived data."""

@@ -354,3 +354,53 @@ def test_chain_batch_checkpoint_resume_is_exact(move, torch_cuda, tmp_path):
         assert torch.equal(getattr(a, name), getattr(b, name)), name
     with pytest.raises(ValueError):
         E.ChainBatch(geo, occ[:2], g["eci"], kT[:2], move, seed=1).load(path)
+
+
+def _check_swap_state(cb, occ0, oracle_mod=None):
+    """Compositions conserved and the per-species site lists (trk / loc) equal to the occupation."""
+    m = cb.geo.model
+    occ = cb.occ.cpu().numpy()
+    trk, loc = cb.trk.cpu().numpy(), cb.loc.cpu().numpy()
+    start, count = cb.trk_start.cpu().numpy(), cb.trk_count.cpu().numpy()
+    for c in range(cb.n_chains):
+        assert np.array_equal(np.bincount(occ[c], minlength=m.n_sym), np.bincount(occ0[c], minlength=m.n_sym))
+        for sp in range(m.n_sym):
+            lst = trk[c, start[c, sp]:start[c, sp] + count[c, sp]]
+            assert set(lst.tolist()) == set(np.nonzero(occ[c] == sp)[0].tolist())
+            assert np.array_equal(loc[c, lst], np.arange(count[c, sp]))
+    if oracle_mod is not None:
+        orc = oracle_mod.Oracle(m)
+        cf = cb.cf.cpu().numpy()
+        for c in range(cb.n_chains):
+            assert np.allclose(cf[c], orc.full_cf(occ[c]), rtol=1e-9, atol=1e-12)
+
+
+def test_graph_capture_keeps_swap_state_consistent(torch_cuda, oracle_mod):
+    """Capturing a runner's step runs one warm step and restores the state; both must be ordered on the
+    runner's stream, or the restore lands in the middle of the (long) warm kernel and leaves site lists
+    that disagree with the occupation."""
+    from cemc_gb300 import engine as E
+    from cemc_gb300.batch import BatchRunner, MultiBatchRunner
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    rng = np.random.default_rng(8)
+    runners, occs = [], []
+    for L in (12, 6):
+        s = fcc_settings(L, 5, 3, 1, ["Al", "Mg", "Si"])
+        eci = seeded_ecis(s.cset, 0)
+        m = CEModel(s, list(eci))
+        geo = E.Geometry(m)
+        occ = rng.integers(0, 3, (3, m.n_sites)).astype(np.int8)
+        occs.append(occ)
+        runners.append(BatchRunner(geo, occ, m.eci_vector(eci), 800.0, E.MOVE_SWAP, seed=2, precision=E.PREC_F32,
+                                   warps=16, cluster=1, sweeps_per_step=20, graph=True))
+    r0 = runners[0]
+    r0.capture()
+    r0.step(2)
+    r0.synchronize()
+    _check_swap_state(r0.cb, occs[0], oracle_mod)
+    multi = MultiBatchRunner(runners)
+    multi.step(2)
+    multi.synchronize()
+    for r, occ in zip(runners, occs):
+        _check_swap_state(r.cb, occ, oracle_mod)
