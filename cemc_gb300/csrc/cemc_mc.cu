@@ -64,6 +64,16 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
+// Hint that the 128-byte line holding p will be read soon (global memory, into L1).
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
+// Every line of one neighbour row of the table.
+__device__ __forceinline__ void prefetch_row(const int32_t *row, int cpad) {
+  const uintptr_t b = reinterpret_cast<uintptr_t>(row) & ~(uintptr_t)127;
+  const uintptr_t e = reinterpret_cast<uintptr_t>(row + cpad);
+  for (uintptr_t q = b; q < e; q += 128) prefetch_l1(reinterpret_cast<const void *>(q));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
@@ -453,6 +463,22 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         d.x0 = w1.v[0];
         d.x1 = w1.v[1];
         d.site = -1;
+        // The sites are read from the site lists when the trial is evaluated, rounds from
+        // now; the lists' extents do not change (swaps keep every species count), so the
+        // sites at the trial's two list slots now are almost always the ones it will
+        // read: warm L1 with their neighbour rows.  Only a hint; a stale guess costs the
+        // L2 latency the evaluation pays without it.
+        const int np = misc[2];
+        if (np >= 2) {
+          const int ia = (int)cemc_below(w0.v[0], (uint32_t)np);
+          int ib = (int)cemc_below(w0.v[1], (uint32_t)(np - 1));
+          ib += (ib >= ia);
+          const int A = misc[4 + ia], B = misc[4 + ib];
+          const int pa = trk[misc[12 + A] + (int)cemc_below(w0.v[2], (uint32_t)misc[20 + A])];
+          const int pb = trk[misc[12 + B] + (int)cemc_below(w0.v[3], (uint32_t)misc[20 + B])];
+          if ((unsigned)pa < (unsigned)N) prefetch_row(g.table + (size_t)pa * cpad, cpad);
+          if ((unsigned)pb < (unsigned)N) prefetch_row(g.table + (size_t)pb * cpad, cpad);
+        }
       } else {
         d.x0 = d.x1 = 0;
         // the flipped site: uniform over the movable sites (all sites without a background)
