@@ -375,11 +375,12 @@ class CE:
 
 
 class SimpleAtom:
-    __slots__ = ("symbol", "index")
+    __slots__ = ("symbol", "index", "tag")
 
-    def __init__(self, symbol, index):
+    def __init__(self, symbol, index, tag=0):
         self.symbol = symbol
         self.index = index
+        self.tag = tag
 
 
 class SimpleAtoms(list):

@@ -533,9 +533,13 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->kernel == CEMC_KERNEL_TABLE && !g.table_ok)
     return fail(CEMC_ERR_LIMIT, "the table kernel needs translation groups of equal size and pattern tables of at "
                                 "most %d entries", cemc::kMaxTable);
-  const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP;
+  // move constraints are checked (and redrawn) by the one-trial-per-warp forms
+  const bool constrained = r->site_allow != nullptr || r->frozen != nullptr;
+  if (r->max_attempts < 0) return fail(CEMC_ERR_ARG, "max_attempts must be >= 0");
+  const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP && !constrained;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
-    return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs single-site flips with at most 16 cluster ECIs");
+    return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs unconstrained single-site flips with at most 16 "
+                              "cluster ECIs");
   // two trials per warp: asked for, or chosen when eligible and no CTA pair was asked for
   // (a CTA pair takes the half-warp form only when that form is asked for explicitly)
   const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
@@ -576,6 +580,9 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   a.chain_key = r->chain_key;
   a.accum_slot = r->accum_slot;
   a.chain_trials = r->chain_trials;
+  a.site_allow = r->site_allow;
+  a.frozen = r->frozen;
+  a.max_attempts = r->max_attempts > 0 ? r->max_attempts : 10000;
   a.tpw = tpw;
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
   // Evaluation forms to try, in order: spin, or table then generic (AUTO), or the one asked for.

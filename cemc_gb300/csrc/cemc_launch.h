@@ -33,6 +33,9 @@ struct RunArgs {
   const int32_t *accum_slot;
   const uint64_t *chain_trials;
   uint64_t chunk_offset;  // trials of this chain already run by earlier chunks of the same call
+  const uint8_t *site_allow;  // move constraints (see cemc_run_desc), NULL = none
+  const uint32_t *frozen;
+  int max_attempts;
 };
 
 constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two or three more warps are helpers

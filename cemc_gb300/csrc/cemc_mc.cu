@@ -137,6 +137,14 @@ __device__ __forceinline__ uint32_t spin_lane_parities(const uint4 *terms, int l
 
 
 
+// ---- move constraints -------------------------------------------------------------
+// A change (site, old -> new) passes the move constraints: species `old` is not
+// frozen (FixedElement) and species `new` may be placed on the site
+// (ConstrainElementByTag, FixEdgeLayers); allow NULL = every species.
+__device__ __forceinline__ bool change_legal(const uint8_t *allow, uint32_t frozen, int site, int old_s, int new_s) {
+  return !((frozen >> old_s) & 1u) && (allow == nullptr || ((allow[site] >> new_s) & 1u));
+}
+
 // ---- table form ---------------------------------------------------------------
 // Species of the neighbour columns of `row` into sp[0..n_cols) (site `ovr` read
 // as species `ovr_s`); each lane keeps the site ids of its columns in nbr[] for
@@ -423,6 +431,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
 
   const double kT = a.kT[chain];
+  // move constraints of this chain (the redraw loop runs only when there are any)
+  const uint8_t *allow = a.site_allow ? a.site_allow + (size_t)chain * N : nullptr;
+  const uint32_t frz = a.frozen ? a.frozen[chain] : 0u;
+  const bool cons = allow != nullptr || frz != 0u;
   const float inv_kT = (float)(1.0 / kT);
   const uint32_t key = a.chain_key ? a.chain_key[chain] : (uint32_t)chain;
   uint64_t my_trials = a.n_trials;
@@ -819,33 +831,74 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           int nbra[4], nbrb[4] = {-1, -1, -1, -1};
           uint32_t ua, ub;
           uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
+          // Move constraints: an illegal proposal is redrawn, proposal k of trial t from
+          // counter streams 2k, 2k + 1, until one is legal or max_attempts redraws are spent
+          // (montecarlo.py:976-988: spending the last redraw fails even if it is legal);
+          // a failed search rejects the trial and marks the chain CEMC_ERR_NO_MOVE.
+          bool no_move = false;
           if (!SWAP) {
             sa = dr.site;
-            const int oa = occ[sa];
-            const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
+            int oa = occ[sa];
+            int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
             na = k + (k >= oa);
             ua = dr.w2;
             ub = dr.w3;
+            const int32_t *frow = rows + (size_t)slot * cpad;  // prefetched by the fetcher
+            if (cons) {
+              int att = 0;
+              while (!change_legal(allow, frz, sa, oa, na) && att < a.max_attempts) {
+                ++att;
+                const cemc_u32x4 w = cemc_trial_draw(a.seed, key, t, (uint32_t)(2 * att));
+                sa = g.n_movable == N ? (int)cemc_below(w.v[0], (uint32_t)N)
+                                      : g.movable[cemc_below(w.v[0], (uint32_t)g.n_movable)];
+                oa = occ[sa];
+                k = (int)cemc_below(w.v[1], (uint32_t)(g.n_sym - 1));
+                na = k + (k >= oa);
+                ua = w.v[2];
+                ub = w.v[3];
+              }
+              no_move = att == a.max_attempts;
+              if (att > 0) frow = g.table + (size_t)sa * cpad;  // a redrawn site's row comes from L2
+            }
             old_a = oa;
             if constexpr (TAB) {
-              table_gather(g, occ, rows + (size_t)slot * cpad, -1, 0, sp_a, nbra, lane);
+              table_gather(g, occ, frow, -1, 0, sp_a, nbra, lane);
             } else if constexpr (!SPIN) {
-              gather_smem_row<R>(g, occ, bf_s, rows + (size_t)slot * cpad, oa, na, va, nbra, lane);
+              gather_smem_row<R>(g, occ, bf_s, frow, oa, na, va, nbra, lane);
             } else {
               occ_a_bit = (uint32_t)oa ^ xorv;
-              spin_ballot(g, occ, rows + (size_t)slot * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+              spin_ballot(g, occ, frow, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
             }
           } else {
-            const int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
+            int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
             int ib = (int)cemc_below(dr.w1, (uint32_t)(n_present - 1));
             ib += (ib >= ia);
             A_ = misc[4 + ia];
             B_ = misc[4 + ib];
             sa = trk[misc[12 + A_] + (int)cemc_below(dr.w2, (uint32_t)misc[20 + A_])];
             sb = trk[misc[12 + B_] + (int)cemc_below(dr.w3, (uint32_t)misc[20 + B_])];
-            na = B_;
             ua = dr.x0;
             ub = dr.x1;
+            if (cons) {
+              int att = 0;
+              while (!(change_legal(allow, frz, sa, A_, B_) && change_legal(allow, frz, sb, B_, A_)) &&
+                     att < a.max_attempts) {
+                ++att;
+                const cemc_u32x4 w = cemc_trial_draw(a.seed, key, t, (uint32_t)(2 * att));
+                const cemc_u32x4 x = cemc_trial_draw(a.seed, key, t, (uint32_t)(2 * att + 1));
+                ia = (int)cemc_below(w.v[0], (uint32_t)n_present);
+                ib = (int)cemc_below(w.v[1], (uint32_t)(n_present - 1));
+                ib += (ib >= ia);
+                A_ = misc[4 + ia];
+                B_ = misc[4 + ib];
+                sa = trk[misc[12 + A_] + (int)cemc_below(w.v[2], (uint32_t)misc[20 + A_])];
+                sb = trk[misc[12 + B_] + (int)cemc_below(w.v[3], (uint32_t)misc[20 + B_])];
+                ua = x.v[0];
+                ub = x.v[1];
+              }
+              no_move = att == a.max_attempts;
+            }
+            na = B_;
             // first half: site a takes B; second half: site b takes A with a already changed
             if constexpr (TAB) {
               table_gather(g, occ, g.table + (size_t)sa * cpad, -1, 0, sp_a, nbra, lane);
@@ -932,7 +985,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           }
           int acc = 0;
           if (lane == 0) {
-            acc = metropolis<R>(de, ua, ub, kT, inv_kT);
+            acc = no_move ? 0 : metropolis<R>(de, ua, ub, kT, inv_kT);
+            if (no_move && a.status) a.status[chain] = CEMC_ERR_NO_MOVE;
             put(&r_sa[gidx], (int32_t)sa);
             put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
             put(&r_acc[gidx], (int8_t)acc);

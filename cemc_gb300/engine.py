@@ -291,12 +291,22 @@ class ChainBatch:
 
     # -- library calls -----------------------------------------------------
     def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
-            chain_trials: Optional[torch.Tensor] = None, kernel: int = 0, cluster: int = 0):
+            chain_trials: Optional[torch.Tensor] = None, kernel: int = 0, cluster: int = 0,
+            site_allow: Optional[torch.Tensor] = None, frozen: Optional[torch.Tensor] = None,
+            max_attempts: int = 0):
         """Run ``n_trials`` trials on every chain in one launch (``cemc_run``).
 
         ``chain_trials`` (device int64, one per chain, each <= n_trials) gives chains their own counts.
         ``warps`` evaluating warps per CTA; ``cluster`` CTAs per chain (1, 2, or 0 = chosen by the library).
+        Move constraints: ``site_allow`` (device uint8 [n_chains, n_sites], bit s = species s may be
+        placed on the site), ``frozen`` (device int32 [n_chains], bit s = a site holding species s may
+        not change), ``max_attempts`` redraws per trial (0 = 10000); see ``mc_constraints``.
         """
+        if site_allow is not None:
+            if site_allow.dtype != torch.uint8 or site_allow.numel() != self.n_chains * self.geo.model.n_sites:
+                raise ValueError("site_allow must be uint8 [n_chains, n_sites]")
+        if frozen is not None and (frozen.dtype != torch.int32 or frozen.numel() != self.n_chains):
+            raise ValueError("frozen must be int32 [n_chains]")
         tr = None
         if trace:
             tr = (torch.zeros(self.n_chains * n_trials * 2, dtype=torch.int32, device=self.occ.device),
@@ -309,7 +319,8 @@ class ChainBatch:
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
                          _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel(),
-                         _ptr(self._stamps()), self._stamp_buf.numel() if self._stamp_buf is not None else 0)
+                         _ptr(self._stamps()), self._stamp_buf.numel() if self._stamp_buf is not None else 0,
+                         0, _ptr(site_allow), _ptr(frozen), int(max_attempts))
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         # the table form ends the call with a full recompute (cf and energy exact already)

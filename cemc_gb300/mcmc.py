@@ -83,6 +83,8 @@ class Montecarlo:
         self.indeces = range(len(atoms)) if indeces is None else indeces
         self.observers = []
         self.constraints = []
+        self.max_allowed_constraint_pass_attempts = int(max_constraint_attempts)
+        self._constraint_dev = None  # device masks of self.constraints, built on first use
         self.bias_potentials = []
         self.current_step = 0
         self.num_accepted = 0
@@ -155,7 +157,84 @@ class Montecarlo:
         self.update_current_energy()
 
     def add_constraint(self, constraint):
-        raise NotImplementedError("move constraints are not supported by the GPU drivers")
+        """Add a move constraint (montecarlo.py:386-392), enforced on the device.
+
+        FixedElement, ConstrainElementByTag and FixEdgeLayers (this package's or the
+        reference's objects) become per-site masks checked by the kernel's redraw loop;
+        other constraints raise ``NotImplementedError`` (see ``mc_constraints``).
+        """
+        from .mc_constraints import device_masks
+        m = self._calc().model
+        device_masks(constraint, m.symbols, m.n_sites)
+        self.constraints.append(constraint)
+        self._constraint_dev = None
+
+    def _no_constraint_violations(self, system_changes):
+        """montecarlo.py:334-347."""
+        for constraint in self.constraints:
+            if not constraint(system_changes):
+                return False
+        return True
+
+    def _constraint_args(self):
+        """Device masks and redraw limit of the constraints, as ``ChainBatch.run`` arguments."""
+        if not self.constraints:
+            return {}
+        if self._constraint_dev is None:
+            from .mc_constraints import combined_masks
+            m = self._calc().model
+            allow, frozen = combined_masks(self.constraints, m.symbols, m.n_sites)
+            dev = self._calc().updater.occ_d.device
+            self._constraint_dev = {
+                "site_allow": None if allow is None else torch.as_tensor(allow[None, :]).to(dev),
+                "frozen": torch.tensor([np.int32(np.uint32(frozen).view(np.int32))], dtype=torch.int32,
+                                       device=dev) if frozen else None,
+            }
+        return dict(self._constraint_dev, max_attempts=self.max_allowed_constraint_pass_attempts)
+
+    def insert_symbol(self, symb, indices):
+        """Put ``symb`` on the given sites (montecarlo.py:219-233); each change must pass the constraints."""
+        calc = self._calc()
+        for indx in indices:
+            change = (int(indx), self.atoms[indx].symbol, symb)
+            if not self._no_constraint_violations([change]):
+                raise ValueError("The indices given results in an update that violate one or more constraints!")
+            calc.update_cf(change)
+        calc.clear_history()
+        self._invalidate_chain()
+        self.symbols = sorted(set(a.symbol for a in self.atoms) | set(self.symbols))
+        self.update_current_energy()
+
+    def insert_symbol_random_places(self, symbol, num=1, swap_symbs=()):
+        """Put ``symbol`` on ``num`` random sites holding one of ``swap_symbs`` (montecarlo.py:235-275).
+
+        Draws from numpy's global generator where the reference uses Python's ``random``.
+        """
+        calc = self._calc()
+        symbs = [a.symbol for a in self.atoms]
+        swap_symbs = list(swap_symbs) if swap_symbs else sorted(set(symbs))
+        max_attempts = 10 * len(self.atoms)
+        num_inserted = attempts = 0
+        while num_inserted < num and attempts < max_attempts:
+            attempts += 1
+            old_symb = swap_symbs[np.random.randint(len(swap_symbs))]
+            if old_symb == symbol:
+                continue
+            sites = [i for i, a in enumerate(self.atoms) if a.symbol == old_symb]
+            if not sites:
+                continue
+            indx = sites[np.random.randint(len(sites))]
+            change = (indx, old_symb, symbol)
+            if not self._no_constraint_violations([change]):
+                continue
+            calc.update_cf(change)
+            num_inserted += 1
+        calc.clear_history()
+        self._invalidate_chain()
+        self.symbols = sorted(set(a.symbol for a in self.atoms) | set(self.symbols))
+        self.update_current_energy()
+        if attempts == max_attempts:
+            raise RuntimeError("Could insert {} {} atoms!".format(num, symbol))
 
     def add_bias(self, potential):
         raise NotImplementedError("bias potentials are not supported by the GPU drivers")
@@ -191,7 +270,7 @@ class Montecarlo:
         done = 0
         while done < n:
             k = min(block, n - done)
-            tr = ch.run(k, precision=self.precision, warps=self._warps(), trace=trace)
+            tr = ch.run(k, precision=self.precision, warps=self._warps(), trace=trace, **self._constraint_args())
             if trace:
                 traces.append(tr)
             if k == block:
@@ -212,7 +291,14 @@ class Montecarlo:
     def _sync_after_run(self):
         ch = self._chain
         torch.cuda.synchronize(ch.occ.device)
-        ch.check_status()
+        try:
+            ch.check_status()
+        except E._lib.CemcError as exc:
+            if exc.code == E._lib.ERR_NO_MOVE:
+                ch.status.zero_()
+                raise CanNotFindLegalMoveError("Did not manage to produce a trial move that does not violate any "
+                                               "of the constraints") from exc
+            raise
         calc = self._calc()
         # mirror the new configuration into the atoms object and drop the undo buffer
         occ = calc.updater.occupation()
@@ -230,7 +316,7 @@ class Montecarlo:
         """One trial (the reference's _mc_step); returns (energy, accepted)."""
         before = self.num_accepted
         ch = self.chain()
-        _, acc, _ = ch.run(1, precision=self.precision, warps=1, trace=True)
+        _, acc, _ = ch.run(1, precision=self.precision, warps=1, trace=True, **self._constraint_args())
         self.current_step += 1
         self._sync_after_run()
         return self.current_energy, bool(acc.cpu().numpy()[0, 0])
@@ -401,7 +487,7 @@ class Montecarlo:
     # -- checkpoint / restart (montecarlo.py:1040-1074) ---------------------------------
     _CHECKPOINT_ATTRS = ("T", "min_acc_rate", "current_step", "num_accepted", "status_every_sec", "energy_bias",
                          "correlation_info", "precision", "warps", "recompute_every_sweeps", "seed", "symbols",
-                         "current_energy", "logfile", "name")
+                         "current_energy", "logfile", "name", "max_allowed_constraint_pass_attempts")
 
     def _checkpoint_attrs(self):
         return self._CHECKPOINT_ATTRS
@@ -415,8 +501,8 @@ class Montecarlo:
         (``ChainBatch.state_dict``: occupation, correlation functions, energy, the
         trial counter of the counter-based stream, the running sums and the swap
         site lists), so a loaded driver draws the same trials and reaches
-        bit-identical states.  Observers are not stored: like the reference does
-        for observers it cannot serialise, the caller attaches them again.
+        bit-identical states.  Observers and constraints are not stored: like the
+        reference does for those it cannot serialise, the caller attaches them again.
         """
         import pickle
         calc = self._calc()

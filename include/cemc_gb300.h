@@ -29,6 +29,8 @@ extern "C" {
 #define CEMC_ERR_LIMIT 5      /* a compiled-in limit was exceeded */
 #define CEMC_ERR_TIMEOUT 6    /* a bounded device wait ran out */
 #define CEMC_ERR_INTERNAL 7   /* a device-side consistency check failed (the chain's state was not written) */
+#define CEMC_ERR_NO_MOVE 8    /* no trial move satisfying the move constraints within max_attempts draws
+                                 (CanNotFindLegalMoveError, montecarlo.py:984-987) */
 
 #define CEMC_MAX_BF 4         /* decorations per site (species - 1) */
 #define CEMC_MAX_ECI 128      /* ECIs per cluster expansion */
@@ -166,6 +168,14 @@ typedef struct {
   uint64_t stamp_words;
   int32_t kernel_used; /* output: the CEMC_KERNEL_* form cemc_run launched (CEMC_KERNEL_TABLE: the call
                           already ended with a full recompute) */
+  /* Move constraints (mc_constraints.py; redraw loop of montecarlo.py:976-988).  A change (site,
+   * old, new) is legal when species `old` is not frozen and species `new` is allowed at `site`;
+   * a move is legal when all its changes are.  An illegal proposal is redrawn (draw k of trial t
+   * uses counter streams 2k, 2k+1) up to max_attempts times; when the redraws run out the trial
+   * is rejected and the chain's status becomes CEMC_ERR_NO_MOVE.  All NULL = unconstrained. */
+  const uint8_t *site_allow;    /* [n_chains * n_sites] bit s: species s may be placed on the site, or NULL */
+  const uint32_t *frozen;       /* [n_chains] bit s: a site holding species s may not change, or NULL */
+  int32_t max_attempts;         /* redraws per trial; 0 = 10000 (the reference's default) */
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when

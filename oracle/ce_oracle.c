@@ -171,6 +171,16 @@ void orc_tracker_init(const orc_model *m, const int8_t *occ, int32_t *trk, int32
   }
 }
 
+/* A change (site, old -> new) passes the constraints: FixedElement blocks a change whose
+ * old symbol is the fixed element (mc_constraints.py:95-107 compares the change's old symbol;
+ * its index field never equals a symbol), ConstrainElementByTag requires the new symbol to be
+ * allowed at the site (187-190), FixEdgeLayers allows no change on a fixed site (156-164). */
+static int change_legal(const orc_chain *c, int site, int old_s, int new_s) {
+  if ((c->frozen >> old_s) & 1u) return 0;
+  if (c->allow && !((c->allow[site] >> new_s) & 1u)) return 0;
+  return 1;
+}
+
 static void accumulate(const orc_model *m, const double *cf, double e, cemc_accum *acc) {
   if (!acc) return;
   const double de = e - acc->e_ref;
@@ -208,33 +218,54 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
   }
   double e_cur = *c->energy;
   int rc = 0;
+  const int constrained = c->allow != NULL || c->frozen != 0;
+  const int max_att = c->max_attempts > 0 ? c->max_attempts : 10000;
   for (uint64_t it = 0; it < n_trials; ++it) {
     const uint64_t t = t_begin + it;
-    const cemc_u32x4 w = cemc_trial_draw(seed, chain_id, t, 0);
     int a, b = -1, na, nb = -1;
     double u;
     double *cf_new;
+    /* Proposal k of trial t uses counter streams 2k (and 2k + 1): an illegal proposal is
+     * redrawn until one is legal or max_att redraws are spent; like the reference
+     * (montecarlo.py:984-987), spending the last redraw ends the search in failure even if
+     * that redraw is legal, and the trial is then rejected with status ORC_ERR_NO_MOVE. */
+    int att = 0, no_move = 0;
     if (move == ORC_MOVE_FLIP) {
-      a = m->movable[cemc_below(w.v[0], (uint32_t)m->n_movable)];
-      const int old = c->occ[a];
-      const int k = (int)cemc_below(w.v[1], (uint32_t)(m->n_sym - 1));
-      na = k + (k >= old);
-      u = cemc_u01_53(w.v[2], w.v[3]);
+      int old;
+      for (;;) {
+        const cemc_u32x4 w = cemc_trial_draw(seed, chain_id, t, (uint32_t)(2 * att));
+        a = m->movable[cemc_below(w.v[0], (uint32_t)m->n_movable)];
+        old = c->occ[a];
+        const int k = (int)cemc_below(w.v[1], (uint32_t)(m->n_sym - 1));
+        na = k + (k >= old);
+        u = cemc_u01_53(w.v[2], w.v[3]);
+        if (!constrained || change_legal(c, a, old, na) || att == max_att) break;
+        ++att;
+      }
+      no_move = constrained && att == max_att;
       orc_update_cf(m, c->occ, a, na, c->cf, next);
       cf_new = next;
     } else {
-      const cemc_u32x4 x = cemc_trial_draw(seed, chain_id, t, 1);
-      const int ia = (int)cemc_below(w.v[0], (uint32_t)n_present);
-      int ib = (int)cemc_below(w.v[1], (uint32_t)(n_present - 1));
-      ib += (ib >= ia);
-      const int A = present[ia], B = present[ib];
-      const int ra = (int)cemc_below(w.v[2], (uint32_t)c->trk_count[A]);
-      const int rb = (int)cemc_below(w.v[3], (uint32_t)c->trk_count[B]);
-      a = c->trk[c->trk_start[A] + ra];
-      b = c->trk[c->trk_start[B] + rb];
+      int A, B;
+      for (;;) {
+        const cemc_u32x4 w = cemc_trial_draw(seed, chain_id, t, (uint32_t)(2 * att));
+        const cemc_u32x4 x = cemc_trial_draw(seed, chain_id, t, (uint32_t)(2 * att + 1));
+        const int ia = (int)cemc_below(w.v[0], (uint32_t)n_present);
+        int ib = (int)cemc_below(w.v[1], (uint32_t)(n_present - 1));
+        ib += (ib >= ia);
+        A = present[ia];
+        B = present[ib];
+        const int ra = (int)cemc_below(w.v[2], (uint32_t)c->trk_count[A]);
+        const int rb = (int)cemc_below(w.v[3], (uint32_t)c->trk_count[B]);
+        a = c->trk[c->trk_start[A] + ra];
+        b = c->trk[c->trk_start[B] + rb];
+        u = cemc_u01_53(x.v[0], x.v[1]);
+        if (!constrained || (change_legal(c, a, A, B) && change_legal(c, b, B, A)) || att == max_att) break;
+        ++att;
+      }
+      no_move = constrained && att == max_att;
       na = B;
       nb = A;
-      u = cemc_u01_53(x.v[0], x.v[1]);
       /* Two sequential single-site updates, the second seeing the first
        * already applied (ce_updater.cpp:845-853). */
       orc_update_cf(m, c->occ, a, B, c->cf, next);
@@ -245,7 +276,10 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
     }
     const double e_new = orc_energy(m, c->eci, cf_new);
     int accept;
-    if (e_new < e_cur) {
+    if (no_move) {
+      accept = 0;
+      rc = ORC_ERR_NO_MOVE;
+    } else if (e_new < e_cur) {
       accept = 1;
     } else {
       const double prob = exp(-(e_new - e_cur) / c->kT);

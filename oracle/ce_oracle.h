@@ -12,6 +12,7 @@
 #define ORC_ERR_ARG 1
 #define ORC_ERR_BACKGROUND 3
 #define ORC_ERR_STATE 4
+#define ORC_ERR_NO_MOVE 8 /* no legal trial move within max_attempts redraws */
 
 /* Reference-shaped model: per-cluster members/order lists and equivalent
  * decorations, as CEUpdater holds them (cpp/include/cluster.hpp:14-54). */
@@ -44,6 +45,12 @@ typedef struct {
   cemc_accum *acc;
   int32_t *trk, *loc;
   const int32_t *trk_start, *trk_count;
+  /* Move constraints (mc_constraints.py, redraw loop montecarlo.py:976-988): a change (site,
+   * old, new) is legal when old is not in `frozen` and new is allowed at the site
+   * (allow[site] bit new; allow NULL = every species).  max_attempts 0 = 10000. */
+  const uint8_t *allow;
+  uint32_t frozen;
+  int32_t max_attempts;
 } orc_chain;
 
 typedef struct {

@@ -48,7 +48,16 @@ class OrcModel(C.Structure):
 
 class OrcChain(C.Structure):
     _fields_ = [("occ", _P), ("cf", _P), ("eci", _P), ("kT", C.c_double), ("energy", _P), ("acc", _P),
-                ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P)]
+                ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
+                ("allow", _P), ("frozen", C.c_uint32), ("max_attempts", C.c_int32)]
+
+
+class NoLegalMove(RuntimeError):
+    """The constraint redraws of a trial ran out (CanNotFindLegalMoveError); ``trace`` holds the run."""
+
+    def __init__(self, trace):
+        super().__init__("no trial move satisfying the constraints within the allowed redraws")
+        self.trace = trace
 
 
 class OrcTrace(C.Structure):
@@ -89,8 +98,8 @@ def lib():
     return _lib
 
 
-def _ptr(a: np.ndarray) -> int:
-    return a.ctypes.data
+def _ptr(a: Optional[np.ndarray]) -> Optional[int]:
+    return None if a is None else a.ctypes.data
 
 
 class Oracle:
@@ -147,8 +156,12 @@ class Oracle:
             raise RuntimeError("Attempting to move a background atom!")
         return out
 
-    def new_chain_state(self, occ: np.ndarray, eci: np.ndarray, kT: float, move: int, e_ref: Optional[float] = None):
-        """Host-side chain (occ, cf from the full recompute, energy, tracker, sums)."""
+    def new_chain_state(self, occ: np.ndarray, eci: np.ndarray, kT: float, move: int, e_ref: Optional[float] = None,
+                        allow: Optional[np.ndarray] = None, frozen: int = 0, max_attempts: int = 0):
+        """Host-side chain (occ, cf from the full recompute, energy, tracker, sums).
+
+        ``allow`` (uint8 per site, bit s = species s may be placed there), ``frozen`` (bit s = a site
+        holding species s may not change) and ``max_attempts`` are the move constraints."""
         m = self.model
         st = types.SimpleNamespace()
         st.occ = np.ascontiguousarray(occ, dtype=np.int8).copy()
@@ -166,11 +179,16 @@ class Oracle:
             self.L.orc_tracker_init(C.byref(self.c), _ptr(st.occ), _ptr(st.trk), _ptr(st.loc), _ptr(st.trk_start),
                                     _ptr(st.trk_count))
         st.move = move
+        st.allow = None if allow is None else np.ascontiguousarray(allow, dtype=np.uint8).copy()
+        st.frozen = int(frozen)
+        st.max_attempts = int(max_attempts)
         return st
 
     def _cchain(self, st) -> OrcChain:
         return OrcChain(_ptr(st.occ), _ptr(st.cf), _ptr(st.eci), st.kT, _ptr(st.energy), _ptr(st.acc),
-                        _ptr(st.trk), _ptr(st.loc), _ptr(st.trk_start), _ptr(st.trk_count))
+                        _ptr(st.trk), _ptr(st.loc), _ptr(st.trk_start), _ptr(st.trk_count),
+                        _ptr(getattr(st, "allow", None)), int(getattr(st, "frozen", 0)),
+                        int(getattr(st, "max_attempts", 0)))
 
     def run(self, st, seed: int, chain_id: int, t_begin: int, n_trials: int, trace: bool = False):
         """Run trials [t_begin, t_begin + n_trials) of one chain in place; optional per-trial trace."""
@@ -184,6 +202,8 @@ class Oracle:
             tr = OrcTrace(_ptr(out.site), _ptr(out.acc), _ptr(out.de), _ptr(out.u))
         rc = self.L.orc_run_chain(C.byref(self.c), C.byref(ch), st.move, seed, chain_id, t_begin, n_trials,
                                   C.byref(tr) if tr is not None else None)
+        if rc == 8:
+            raise NoLegalMove(out)
         if rc:
             raise RuntimeError("oracle run failed with status %d" % rc)
         return out

@@ -159,10 +159,88 @@ def build_case(name, L, ps, ts, qs, syms, move, T, n, seed, background, lattice=
     )
 
 
+def build_constraint_verdicts():
+    """Verdicts of the reference's own constraint classes (mc_constraints.py) on random moves.
+
+    Loads cemc/mcmc/mc_constraints.py and cemc/tools/geometry.py from the reference tree
+    by path (they import only numpy) and asks FixedElement, ConstrainElementByTag and
+    FixEdgeLayers about random single-site changes and swaps of a ternary FCC 4x4x4 cell.
+    """
+    import importlib.util
+    import types
+    ref = os.environ.get("CEMC_REFERENCE", "/root/reference")
+
+    def load(name, rel):
+        spec = importlib.util.spec_from_file_location(name, os.path.join(ref, rel))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+        return mod
+
+    for pkg in ("cemc", "cemc.tools"):
+        sys.modules.setdefault(pkg, types.ModuleType(pkg))
+    geom = load("cemc.tools.geometry", "cemc/tools/geometry.py")
+    sys.modules["cemc.tools"].geometry = geom
+    mc_cons = load("ref_mc_constraints", "cemc/mcmc/mc_constraints.py")
+
+    syms = ["Al", "Mg", "Si"]
+    s = fcc_settings(4, 3, 2, 0, syms)
+    n = s.n_sites
+    a = s.cell.a
+    pos = s.cell.positions.astype(np.float64) * (a / 2.0)
+    cell = np.eye(3) * (a * s.cell.L)
+
+    class Atom:
+        def __init__(self, index, tag):
+            self.index, self.tag = index, tag
+
+    class Atoms(list):
+        def get_cell(self):
+            return cell
+
+        def get_positions(self):
+            return pos
+
+    tags = np.arange(n) % 4
+    element_by_tag = [["Al", "Mg"], ["Mg"], ["Al", "Si"], ["Al", "Mg", "Si"]]
+    atoms = Atoms(Atom(i, int(tags[i])) for i in range(n))
+    thickness = 3.0
+    cons = [mc_cons.FixedElement(element="Mg"), mc_cons.ConstrainElementByTag(atoms, element_by_tag),
+            mc_cons.FixEdgeLayers(thickness=thickness, atoms=atoms)]
+    rng = np.random.default_rng(33)
+    occ = rng.integers(0, 3, n)
+    n_moves = 600
+    moves = np.full((n_moves, 2, 3), -1, dtype=np.int32)  # up to two changes (site, old id, new id)
+    verdict = np.zeros((n_moves, len(cons)), dtype=np.int8)
+    for k in range(n_moves):
+        if k % 2 == 0:
+            i = int(rng.integers(n))
+            new = int((occ[i] + 1 + rng.integers(2)) % 3)
+            ch = [(i, int(occ[i]), new)]
+        else:
+            i, j = (int(x) for x in rng.choice(n, 2, replace=False))
+            while occ[i] == occ[j]:
+                j = int(rng.integers(n))
+            ch = [(i, int(occ[i]), int(occ[j])), (j, int(occ[j]), int(occ[i]))]
+        for q, c in enumerate(ch):
+            moves[k, q] = c
+        changes = [(c[0], syms[c[1]], syms[c[2]]) for c in ch]
+        verdict[k] = [bool(con(changes)) for con in cons]
+    return dict(symbols=np.array(syms), positions=pos, cell=cell, tags=tags,
+                element_by_tag=np.array(["|".join(e) for e in element_by_tag]), fixed_element=np.array("Mg"),
+                thickness=np.array(thickness), moves=moves, verdict=verdict,
+                constraint_names=np.array(["FixedElement", "ConstrainElementByTag", "FixEdgeLayers"]))
+
+
 def main():
     import contextlib
     out_dir = HERE
     only = set(sys.argv[1:])  # case names to (re)generate; default all
+    if not only or "constraints" in only:
+        data = build_constraint_verdicts()
+        np.savez_compressed(os.path.join(out_dir, "constraints_verdicts.npz"), **data)
+        print("constraints_verdicts: %d moves, legal fractions %s" % (len(data["verdict"]),
+                                                                     data["verdict"].mean(axis=0).round(3)))
     for case in CASES:
         if only and case[0] not in only:
             continue

@@ -1,0 +1,136 @@
+"""Move constraints: this package's classes and device masks against the reference's own verdicts
+(tests/golden/constraints_verdicts.npz, recorded from cemc/mcmc/mc_constraints.py), and the oracle's
+redraw loop against a restatement of the reference's loop (montecarlo.py:976-988) on the host."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, KB
+
+
+def _fixture():
+    d = np.load(os.path.join(GOLDEN, "constraints_verdicts.npz"), allow_pickle=False)
+    return {k: d[k] for k in d.files}
+
+
+class _Atom:
+    def __init__(self, index, tag):
+        self.index, self.tag = index, tag
+
+
+def _atoms(g):
+    class Atoms(list):
+        def get_cell(self):
+            return g["cell"]
+
+        def get_positions(self):
+            return g["positions"]
+
+    return Atoms(_Atom(i, int(t)) for i, t in enumerate(g["tags"]))
+
+
+def _ours(g):
+    from cemc_gb300.mc_constraints import ConstrainElementByTag, FixEdgeLayers, FixedElement
+    atoms = _atoms(g)
+    ebt = [str(e).split("|") for e in g["element_by_tag"]]
+    return [FixedElement(element=str(g["fixed_element"])), ConstrainElementByTag(atoms, ebt),
+            FixEdgeLayers(thickness=float(g["thickness"]), atoms=atoms)]
+
+
+def _changes(g, k):
+    syms = [str(s) for s in g["symbols"]]
+    return [(int(c[0]), syms[c[1]], syms[c[2]]) for c in g["moves"][k] if c[0] >= 0]
+
+
+def test_constraint_classes_match_reference_verdicts():
+    g = _fixture()
+    cons = _ours(g)
+    for k in range(len(g["moves"])):
+        ch = _changes(g, k)
+        for q, c in enumerate(cons):
+            assert bool(c(ch)) == bool(g["verdict"][k, q]), (k, g["constraint_names"][q])
+
+
+def test_device_masks_match_reference_verdicts():
+    """A move is legal on the device when every change's old species is not frozen and its new species
+    is allowed at its site: the same verdicts as the reference's objects, one constraint at a time."""
+    from cemc_gb300.mc_constraints import PairConstraint, device_masks
+    g = _fixture()
+    syms = [str(s) for s in g["symbols"]]
+    n = len(g["tags"])
+    for q, c in enumerate(_ours(g)):
+        allow, frozen = device_masks(c, syms, n)
+        for k in range(len(g["moves"])):
+            legal = True
+            for site, old, new in (tuple(int(x) for x in m) for m in g["moves"][k] if m[0] >= 0):
+                if (frozen >> old) & 1 or (allow is not None and not (int(allow[site]) >> new) & 1):
+                    legal = False
+            assert legal == bool(g["verdict"][k, q]), (k, g["constraint_names"][q])
+    with pytest.raises(NotImplementedError):
+        device_masks(PairConstraint(), syms, n)
+
+
+def _redraw_flip(rng_mod, seed, key, t, occ, movable, n_sym, allow, frozen, max_att):
+    """Host restatement of the device redraw loop for a flip (proposal k from counter stream 2k)."""
+    att = 0
+    while True:
+        w = rng_mod.trial_draw(seed, key, t, 2 * att)
+        site = int(movable[rng_mod.below(w[0], len(movable))])
+        old = int(occ[site])
+        k = rng_mod.below(w[1], n_sym - 1)
+        new = k + (k >= old)
+        legal = not (frozen >> old) & 1 and (allow is None or (int(allow[site]) >> new) & 1)
+        if legal or att == max_att:
+            return site, new, att == max_att
+        att += 1
+
+
+def test_oracle_redraw_loop_follows_the_reference(oracle_mod):
+    """Every trial of a constrained oracle run proposes the first legal redraw (or fails after
+    max_attempts, then rejected); the chain never changes a frozen or disallowed site."""
+    from cemc_gb300 import rng as R
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(4, 3, 2, 0, ["Al", "Mg", "Si"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(4)
+    occ0 = rng.integers(0, 3, m.n_sites).astype(np.int8)
+    # Mg sites never change and no Mg is inserted (FixedElement alone lets the element in but never
+    # out, which freezes ever more sites), 60 fixed sites, no Si on one sublattice
+    allow = np.full(m.n_sites, 0b101, dtype=np.uint8)
+    allow[rng.choice(m.n_sites, 60, replace=False)] = 0
+    allow[np.arange(m.n_sites) % 4 == 1] &= 0b001
+    frozen = 1 << 1
+    st = orc.new_chain_state(occ0, m.eci_vector(eci), KB * 900.0, 0, allow=allow, frozen=frozen, max_attempts=50)
+    occ = occ0.copy()
+    n = 3000
+    tr = orc.run(st, seed=9, chain_id=3, t_begin=0, n_trials=n, trace=True)
+    for t in range(n):
+        site, new, failed = _redraw_flip(R, 9, 3, t, occ, m.movable, m.n_sym, allow, frozen, 50)
+        assert (tr.site[2 * t], tr.site[2 * t + 1]) == (site, new)
+        assert not failed
+        if tr.acc[t]:
+            occ[site] = new
+    assert np.array_equal(st.occ, occ)
+    changed = occ != occ0
+    assert not np.any(changed & (allow == 0)) and not np.any(changed & (occ0 == 1))
+    assert not np.any((occ == 2) & (occ0 != 2) & (np.arange(m.n_sites) % 4 == 1))
+
+
+def test_oracle_reports_exhausted_redraws(oracle_mod):
+    """No legal move at all: every trial fails after max_attempts redraws and is rejected."""
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(4, 3, 2, 0, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    orc = oracle_mod.Oracle(m)
+    occ = (np.arange(m.n_sites) % 2).astype(np.int8)
+    st = orc.new_chain_state(occ, m.eci_vector(eci), KB * 900.0, 1, frozen=0b01, max_attempts=5)
+    with pytest.raises(oracle_mod.NoLegalMove) as ei:
+        orc.run(st, seed=1, chain_id=0, t_begin=0, n_trials=20, trace=True)
+    assert not ei.value.trace.acc.any()
+    assert np.array_equal(st.occ, occ)

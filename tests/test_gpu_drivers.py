@@ -404,3 +404,50 @@ def test_graph_capture_keeps_swap_state_consistent(torch_cuda, oracle_mod):
     multi.synchronize()
     for r, occ in zip(runners, occs):
         _check_swap_state(r.cb, occ, oracle_mod)
+
+
+def test_rocksalt_canonical_run_with_fixed_background_element(torch_cuda):
+    """The reference's tests/test_sgc_mc.py:140-191: Li/V on one sublattice, O on the other (background),
+    some V replaced by Li, Montecarlo with FixedElement("O"), a short fixed-mode runMC; O never moves."""
+    from cemc_gb300.calculator import CE, SimpleAtoms
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis, with_background
+    from cemc_gb300.mc_constraints import FixedElement
+    from cemc_gb300.mcmc import Montecarlo
+    s = with_background(fcc_settings(3, 3, 2, 1, ["Li", "V"]), "O")
+    eci = seeded_ecis(s.base.cset, 0)
+    atoms = SimpleAtoms(s.symbols_with_background(["V"] * s.base.n_sites))
+    CE(atoms, s, eci=dict(eci))
+    mc = Montecarlo(atoms, 800, seed=4)
+    mc.add_constraint(FixedElement(element="O"))
+    mc.insert_symbol("Li", [i for i, a in enumerate(atoms) if a.symbol == "V"][:5])
+    mc.runMC(steps=100, equil=False, mode="fixed")
+    syms = [a.symbol for a in atoms]
+    assert all(syms[i] == "O" for i in s.background_indices)
+    assert sum(1 for x in syms if x == "Li") == 5
+
+
+def test_sgc_constraints_by_tag_and_fixed_element(torch_cuda):
+    """SGC flips under ConstrainElementByTag (Si only on one sublattice) and FixedElement("Mg") (sites
+    holding Mg never change): after runMC every site obeys both."""
+    from cemc_gb300.mc_constraints import ConstrainElementByTag, FixedElement
+    from cemc_gb300.mcmc import CanNotFindLegalMoveError, SGCMonteCarlo
+    atoms, calc, s, eci = _calc(recipe=(4, 3, 2, 0, ("Al", "Mg", "Si")), seed=6)
+    for a in atoms:
+        a.tag = a.index % 4
+    before = [a.symbol for a in atoms]
+    mc = SGCMonteCarlo(atoms, 1000.0, seed=12)
+    mc.add_constraint(ConstrainElementByTag(atoms, [["Al", "Mg", "Si"], ["Al", "Mg"], ["Al", "Mg"], ["Al", "Mg"]]))
+    mc.add_constraint(FixedElement(element="Mg"))
+    mc.runMC(steps=4000, chem_potential={"c1_0": 0.0, "c1_1": 0.0}, equil=False)
+    after = [a.symbol for a in atoms]
+    for i, (b, x) in enumerate(zip(before, after)):
+        if b == "Mg":
+            assert x == "Mg"
+        if x != b:
+            assert x != "Si" or i % 4 == 0
+    # no legal move at all: every species frozen
+    mc2 = SGCMonteCarlo(atoms, 1000.0, seed=1)
+    for sym in ("Al", "Mg", "Si"):
+        mc2.add_constraint(FixedElement(element=sym))
+    with pytest.raises(CanNotFindLegalMoveError):
+        mc2._run_trials(10)

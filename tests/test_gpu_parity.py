@@ -428,3 +428,82 @@ def test_gpu_global_stamp_tables_match_oracle(move, E, oracle_mod, monkeypatch):
         assert np.array_equal(acc.cpu().numpy()[0], tr.acc)
         assert np.array_equal(cb.occ.cpu().numpy()[0], st.occ)
         assert _cf_close(cb.cf.cpu().numpy()[0], st.cf)
+
+
+def _constraint_masks(m, n_chains, rng):
+    """Per-chain constraints: fixed sites; no species 1 on one sublattice; (ternary) species 0 frozen and
+    never placed; the last chain unconstrained."""
+    full = (1 << m.n_sym) - 1
+    allow = np.full((n_chains, m.n_sites), full, dtype=np.uint8)
+    frozen = np.zeros(n_chains, dtype=np.int32)
+    allow[0, rng.choice(m.n_sites, m.n_sites // 5, replace=False)] = 0
+    allow[1, np.arange(m.n_sites) % 4 == 0] &= np.uint8(full & ~0b10)
+    if m.n_sym > 2:
+        frozen[1] = 0b1
+        allow[1] &= np.uint8(full & ~0b1)
+    return allow, frozen
+
+
+@pytest.mark.parametrize("kernel", [1, 2, 4])
+@pytest.mark.parametrize("move", [0, 1])
+@pytest.mark.parametrize("case", ["binary_flip", "ternary_swap"])
+def test_gpu_constrained_runs_match_oracle(case, move, kernel, E, oracle_mod):
+    """Move constraints (redraw loop of montecarlo.py:976-988 on per-site masks): every chain's
+    proposals, decisions, occupation and correlation functions equal the oracle's."""
+    import torch
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E, move)
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(11)
+    n_chains = 3
+    occ = rng.integers(0, m.n_sym, (n_chains, m.n_sites)).astype(np.int8)
+    allow, frozen = _constraint_masks(m, n_chains, rng)
+    Ts = np.array([600.0, 900.0, 1200.0])
+    keys = [5, 8, 2]
+    cb = E.ChainBatch(geo, occ, g["eci"], KB * Ts, move, seed=41, chain_keys=keys)
+    n = 2000
+    sites, acc, de = cb.run(n, precision=E.PREC_F64, warps=8, trace=True, kernel=kernel,
+                            site_allow=torch.as_tensor(allow).cuda(), frozen=torch.as_tensor(frozen).cuda(),
+                            max_attempts=300)
+    _sync()
+    cb.check_status()
+    assert cb.last_kernel == kernel
+    sites, acc = sites.cpu().numpy(), acc.cpu().numpy()
+    for c in range(n_chains):
+        st = orc_state = oracle_mod.Oracle(m).new_chain_state(
+            occ[c], g["eci"], KB * Ts[c], move, allow=None if c == 2 else allow[c], frozen=int(frozen[c]),
+            max_attempts=300)
+        tr = oracle_mod.Oracle(m).run(orc_state, seed=41, chain_id=keys[c], t_begin=0, n_trials=n, trace=True)
+        assert np.array_equal(sites[c].reshape(-1), tr.site), c
+        assert np.array_equal(acc[c], tr.acc), c
+        assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ), c
+        assert _cf_close(cb.cf.cpu().numpy()[c], st.cf), c
+        changed = st.occ != occ[c]
+        assert not np.any(changed & (allow[c] == 0))
+
+
+@pytest.mark.parametrize("kernel", [1, 4])
+def test_gpu_constraints_without_legal_move_report_status(kernel, E, oracle_mod):
+    """A binary canonical chain with one species frozen has no legal swap: every trial is rejected after
+    max_attempts redraws, the chain is untouched and its status is CEMC_ERR_NO_MOVE."""
+    import torch
+    from cemc_gb300._lib import CemcError, ERR_NO_MOVE
+    g = load_golden("binary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    occ = g["occ0"][None]
+    cb = E.ChainBatch(geo, occ, g["eci"], float(g["kT"]), 1, seed=3)
+    cf0 = cb.cf.clone()
+    _, acc, _ = cb.run(50, precision=E.PREC_F64, warps=4, trace=True, kernel=kernel,
+                       frozen=torch.tensor([0b01], dtype=torch.int32, device="cuda"), max_attempts=7)
+    _sync()
+    with pytest.raises(CemcError) as ei:
+        cb.check_status()
+    assert ei.value.code == ERR_NO_MOVE
+    assert not acc.cpu().numpy().any()
+    assert np.array_equal(cb.occ.cpu().numpy(), occ)
+    assert torch.equal(cb.cf, cf0)
+    st = oracle_mod.Oracle(m).new_chain_state(occ[0], g["eci"], float(g["kT"]), 1, frozen=0b01, max_attempts=7)
+    with pytest.raises(oracle_mod.NoLegalMove):
+        oracle_mod.Oracle(m).run(st, seed=3, chain_id=0, t_begin=0, n_trials=50)
