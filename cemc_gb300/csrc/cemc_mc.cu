@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int32_t *gstart_s = reinterpret_cast<int32_t *>(smem + L.grp + 8 * CEMC_MAX_GROUPS);  // [groups + 1]
   int8_t *kind_s = reinterpret_cast<int8_t *>(smem + L.kind);
   int8_t *dec_s = kind_s + n_eci;
-  // misc: [1] status, [2] species present, [4..12) present ids, [12..20) site-list
+  // misc: [1] status, [2] species present, [3] a trial ran out of constraint redraws, [4..12) present ids, [12..20) site-list
   //       starts, [20..28) site-list counts, [32..36) round starts written by the peer CTA,
   //       [36..40) accept counts of this CTA's bookers
   int32_t *misc = reinterpret_cast<int32_t *>(smem + L.misc);
@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
   if (tid == 0) {
     misc[1] = 0;
+    misc[3] = 0;
     t0_slot[0] = t0_slot[1] = 0;
     nacc_slot[0] = nacc_slot[1] = 0;
     if (SWAP) {
@@ -986,7 +987,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           int acc = 0;
           if (lane == 0) {
             acc = no_move ? 0 : metropolis<R>(de, ua, ub, kT, inv_kT);
-            if (no_move && a.status) a.status[chain] = CEMC_ERR_NO_MOVE;
+            if (no_move) put(&misc[3], 1);  // reported in the status at the end of the launch
             put(&r_sa[gidx], (int32_t)sa);
             put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
             put(&r_acc[gidx], (int8_t)acc);
@@ -1169,7 +1170,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       ac->n_samples += my_trials;
       ac->n_accept += n_acc_total;
     }
-    if (a.status) a.status[chain] = 0;
+    if (a.status) a.status[chain] = misc[3] ? CEMC_ERR_NO_MOVE : 0;
   }
 }
 

@@ -300,11 +300,10 @@ class Montecarlo:
                                                "of the constraints") from exc
             raise
         calc = self._calc()
-        # mirror the new configuration into the atoms object and drop the undo buffer
-        occ = calc.updater.occupation()
-        syms = calc.model.symbols
-        for i, a in enumerate(self.atoms):
-            s = syms[int(occ[i])]
+        # mirror the new configuration into the atoms object (background sites keep their symbol)
+        # and drop the undo buffer
+        syms = calc.model.symbols_of(calc.updater.occupation())
+        for a, s in zip(self.atoms, syms):
             if a.symbol != s:
                 a.symbol = s
         calc.updater.clear()
