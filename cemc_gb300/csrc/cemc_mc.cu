@@ -432,9 +432,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   }
 
   const double kT = a.kT[chain];
-  // move constraints of this chain (the redraw loop runs only when there are any)
-  const uint8_t *allow = a.site_allow ? a.site_allow + (size_t)chain * N : nullptr;
-  const uint32_t frz = a.frozen ? a.frozen[chain] : 0u;
+  // move constraints of this chain (the redraw loop runs only when there are any; the half-warp
+  // form takes no constraints, and keeping these out of it at compile time keeps its code as fast)
+  const uint8_t *allow = (TPW == 1 && a.site_allow) ? a.site_allow + (size_t)chain * N : nullptr;
+  const uint32_t frz = (TPW == 1 && a.frozen) ? a.frozen[chain] : 0u;
   const bool cons = allow != nullptr || frz != 0u;
   const float inv_kT = (float)(1.0 / kT);
   const uint32_t key = a.chain_key ? a.chain_key[chain] : (uint32_t)chain;
@@ -1170,7 +1171,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       ac->n_samples += my_trials;
       ac->n_accept += n_acc_total;
     }
-    if (a.status) a.status[chain] = misc[3] ? CEMC_ERR_NO_MOVE : 0;
+    if (a.status) a.status[chain] = (TPW == 1 && misc[3]) ? CEMC_ERR_NO_MOVE : 0;
   }
 }
 
