@@ -770,3 +770,282 @@ def l12_settings(L: int, pair_shells: int, triplet_shells: int, quad_shells: int
     """FCC supercell of ``L^3`` cubes with the sublattices as translation-symmetry groups."""
     return SublatticeSettings(FCCSupercell(L, a), enumerate_l12_cluster_types(pair_shells, triplet_shells,
                                                                               quad_shells), symbols, group_of_basis)
+
+
+# ---------------------------------------------------------------------------
+# Hexagonal close-packed crystals.  Positions are integer coordinates in sixths
+# of the hexagonal cell vectors a1 = a (1, 0, 0), a2 = a (-1/2, sqrt(3)/2, 0),
+# a3 = (0, 0, c) with the ideal c / a = sqrt(8/3); the two atoms of the cell sit
+# at (0, 0, 0) and (2, 4, 3).  Squared distances are Q(u, v, w) = 3 (u^2 - uv +
+# v^2) + 8 w^2 = 108 |r|^2 / a^2 (nearest neighbours: Q = 108).  The space group
+# P6_3/mmc is non-symmorphic: its operations pair the 24 hexagonal point
+# operations with fractional translations, and the two atoms of the cell are
+# related by a screw, not by a lattice translation, so an HCP supercell has two
+# translation-symmetry groups that share cluster names (CLEASE's convention for
+# HCP, which the reference takes as given).
+
+_HCP_BASIS = np.array([(0, 0, 0), (2, 4, 3)], dtype=np.int64)
+_HEX_PERIOD = 6
+
+
+def _hex_metric(v: np.ndarray) -> np.ndarray:
+    v = np.asarray(v, dtype=np.int64)
+    return 3 * (v[..., 0] ** 2 - v[..., 0] * v[..., 1] + v[..., 1] ** 2) + 8 * v[..., 2] ** 2
+
+
+def _hex_point_group() -> List[np.ndarray]:
+    """The 24 operations of 6/mmm as integer matrices on lattice coordinates (closure of 6, m, m_z)."""
+    rot = np.array([[1, -1, 0], [1, 0, 0], [0, 0, 1]], dtype=np.int64)  # a1 -> a1 + a2, a2 -> -a1
+    swap = np.array([[0, 1, 0], [1, 0, 0], [0, 0, 1]], dtype=np.int64)
+    zflip = np.diag([1, 1, -1]).astype(np.int64)
+    group = {tuple(np.eye(3, dtype=np.int64).ravel())}
+    frontier = list(group)
+    while frontier:
+        nxt = []
+        for g in frontier:
+            G = np.array(g).reshape(3, 3)
+            for h in (rot, swap, zflip):
+                key = tuple((h @ G).ravel())
+                if key not in group:
+                    group.add(key)
+                    nxt.append(key)
+        frontier = nxt
+    return [np.array(g).reshape(3, 3) for g in sorted(group)]
+
+
+def _hcp_space_group() -> List[Tuple[np.ndarray, np.ndarray]]:
+    """(R, t) with R a point operation and t a translation (sixths) mapping the atom set onto itself."""
+    basis = {tuple(b) for b in _HCP_BASIS.tolist()}
+    ops = []
+    for R in _hex_point_group():
+        img = _HCP_BASIS @ R.T
+        for t in itertools.product(range(_HEX_PERIOD), repeat=3):
+            moved = {tuple(np.mod(p + np.array(t), _HEX_PERIOD).tolist()) for p in img}
+            if moved == basis:
+                ops.append((R, np.array(t, dtype=np.int64)))
+    return ops
+
+
+_HCP_OPS = None
+
+
+def _hcp_ops():
+    global _HCP_OPS
+    if _HCP_OPS is None:
+        _HCP_OPS = _hcp_space_group()
+    return _HCP_OPS
+
+
+def _hcp_canonical_key(points: np.ndarray) -> Tuple:
+    best = None
+    for R, t in _hcp_ops():
+        img = points @ R.T + t
+        for q in img:
+            shift = q - np.mod(q, _HEX_PERIOD)
+            key = tuple(sorted(map(tuple, (img - shift).tolist())))
+            if best is None or key < best:
+                best = key
+    return best
+
+
+def _hcp_maps(src: np.ndarray, dst: np.ndarray):
+    dst_set = {tuple(p): q for q, p in enumerate(dst.tolist())}
+    n = len(src)
+    for R, t in _hcp_ops():
+        img = src @ R.T + t
+        for p0 in dst:
+            shift = p0 - img[0]
+            if np.any(np.mod(shift, _HEX_PERIOD)):
+                continue
+            mapping = [dst_set.get(tuple(p)) for p in (img + shift).tolist()]
+            if None in mapping or len(set(mapping)) != n:
+                continue
+            yield mapping
+
+
+def _hcp_order(points: np.ndarray, proto: np.ndarray) -> List[int]:
+    for mapping in _hcp_maps(points, proto):
+        order = [0] * len(points)
+        for idx, q in enumerate(mapping):
+            order[q] = idx
+        return order
+    raise RuntimeError("sub-cluster is not equivalent to its prototype")
+
+
+def _hcp_equiv_sites(proto: np.ndarray) -> List[List[int]]:
+    n = len(proto)
+    parent = list(range(n))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+
+    for mapping in _hcp_maps(proto, proto):
+        for q in range(n):
+            a, b = find(q), find(mapping[q])
+            if a != b:
+                parent[a] = b
+    groups: Dict[int, List[int]] = {}
+    for q in range(n):
+        groups.setdefault(find(q), []).append(q)
+    return [sorted(gq) for gq in sorted(groups.values()) if len(gq) >= 2]
+
+
+def hcp_shell_radii(max_shell: int) -> List[int]:
+    """Squared distances Q of the first neighbour shells of an HCP site (108 = nearest neighbours)."""
+    rng = np.arange(-4, 5)
+    cells = np.array(list(itertools.product(rng, rng, rng)), dtype=np.int64) * _HEX_PERIOD
+    pts = (cells[:, None, :] + _HCP_BASIS[None, :, :]).reshape(-1, 3)
+    q = np.unique(_hex_metric(pts))
+    return [int(x) for x in q[q > 0][:max_shell]]
+
+
+def enumerate_hcp_cluster_types(pair_shells: int, triplet_shells: int,
+                                quad_shells: int) -> List[SublatticeClusterType]:
+    """Cluster types of the HCP crystal (space group P6_3/mmc) seen from its two atoms."""
+    max_shell = max(pair_shells, triplet_shells, quad_shells, 1)
+    radii = hcp_shell_radii(max_shell)
+    rng = np.arange(-4, 5)
+    cells = np.array(list(itertools.product(rng, rng, rng)), dtype=np.int64) * _HEX_PERIOD
+    all_pts = (cells[:, None, :] + _HCP_BASIS[None, :, :]).reshape(-1, 3)
+    n_groups = len(_HCP_BASIS)
+    types: List[SublatticeClusterType] = []
+    for size, n_shells in ((2, pair_shells), (3, triplet_shells), (4, quad_shells)):
+        if n_shells <= 0:
+            continue
+        cutoff = radii[n_shells - 1]
+        found: Dict[Tuple, SublatticeClusterType] = {}
+        for b, ref in enumerate(_HCP_BASIS):
+            d = _hex_metric(all_pts - ref)
+            nbrs = all_pts[(d > 0) & (d <= cutoff)]
+            nbrs = nbrs[np.lexsort(nbrs.T[::-1])]
+            for combo in itertools.combinations(range(len(nbrs)), size - 1):
+                pts = np.vstack([ref[None, :], nbrs[list(combo)]])
+                diff = pts[:, None, :] - pts[None, :, :]
+                dia2 = int(_hex_metric(diff).max())
+                if dia2 > cutoff:
+                    continue
+                key = _hcp_canonical_key(pts)
+                ct = found.get(key)
+                if ct is None:
+                    proto = np.array(key, dtype=np.int64)
+                    ct = SublatticeClusterType("", size, dia2, proto, _hcp_equiv_sites(proto),
+                                               [[] for _ in range(n_groups)], [[] for _ in range(n_groups)])
+                    found[key] = ct
+                ct.members[b].append(pts[1:].copy())
+                ct.orders[b].append(_hcp_order(pts, ct.prototype))
+        cts = sorted(found.values(), key=lambda c: (c.dia2, sum(len(m) for m in c.members), c.prototype.tolist()))
+        dias = sorted({c.dia2 for c in cts})
+        variant: Dict[int, int] = {}
+        for c in cts:
+            di = dias.index(c.dia2)
+            v = variant.get(di, 0)
+            variant[di] = v + 1
+            c.name = "c%d_d%04d_%d" % (size, di, v)
+            types.append(c)
+    return types
+
+
+class HCPSupercell:
+    """``L x L x Lz`` hexagonal cells of an HCP crystal (2 sites per cell), cell-major site order."""
+
+    def __init__(self, L: int, Lz: int, a: float = 3.21):
+        if L < 1 or Lz < 1:
+            raise ValueError("supercell size must be positive")
+        self.L, self.Lz, self.a = int(L), int(Lz), float(a)
+        self.c = self.a * math.sqrt(8.0 / 3.0)
+        self.period = np.array([L, L, Lz], dtype=np.int64) * _HEX_PERIOD
+        cells = np.array(list(itertools.product(range(L), range(L), range(Lz))), dtype=np.int64)
+        self.positions = ((_HEX_PERIOD * cells)[:, None, :] + _HCP_BASIS[None, :, :]).reshape(-1, 3)
+        self.n_sites = len(self.positions)
+
+    def index_of(self, pos: np.ndarray) -> np.ndarray:
+        p = np.mod(pos, self.period)
+        cell = p // _HEX_PERIOD
+        rem = p % _HEX_PERIOD
+        b = np.full(p.shape[:-1], -1, dtype=np.int64)
+        for i, base in enumerate(_HCP_BASIS.tolist()):
+            b[(rem == base).all(-1)] = i
+        if np.any(b < 0):
+            raise ValueError("position is not an HCP site")
+        return ((cell[..., 0] * self.L + cell[..., 1]) * self.Lz + cell[..., 2]) * len(_HCP_BASIS) + b
+
+    def cartesian(self) -> np.ndarray:
+        """Site positions in angstrom."""
+        f = self.positions.astype(np.float64) / _HEX_PERIOD
+        a1 = np.array([self.a, 0.0, 0.0])
+        a2 = np.array([-0.5 * self.a, 0.5 * math.sqrt(3.0) * self.a, 0.0])
+        a3 = np.array([0.0, 0.0, self.c])
+        return f[:, :1] * a1 + f[:, 1:2] * a2 + f[:, 2:3] * a3
+
+
+class HCPSettings:
+    """Settings object of an HCP supercell: two translation-symmetry groups (the two atoms of the
+    hexagonal cell), one ``cluster_info`` dict per group; same attribute formats as ``Settings``."""
+
+    def __init__(self, cell: HCPSupercell, types: List[SublatticeClusterType], symbols: Sequence[str]):
+        self.cell = cell
+        self.unique_elements = sorted(symbols)
+        self.num_unique_elements = len(self.unique_elements)
+        self.cset = ClusterSet(types, self.num_unique_elements - 1)
+        if self.num_unique_elements == 2:
+            self.basis_functions = binary_basis(self.unique_elements)
+        elif self.num_unique_elements == 3:
+            self.basis_functions = ternary_basis(self.unique_elements)
+        else:
+            raise ValueError("only binary and ternary alloys are generated")
+        n = cell.n_sites
+        self.n_sites = n
+        nb = len(_HCP_BASIS)
+        basis_of = np.arange(n) % nb
+        self.index_by_trans_symm = [np.nonzero(basis_of == b)[0].tolist() for b in range(nb)]
+        self.background_indices: List[int] = []
+        info: List[Dict[str, dict]] = []
+        col_set = set()
+        for b in range(nb):
+            d: Dict[str, dict] = {}
+            offs = set()
+            for t in types:
+                if not t.members[b]:
+                    continue
+                idx = [cell.index_of(mm).astype(np.int64).tolist() for mm in t.members[b]]
+                for row in idx:
+                    if len(set(row)) != len(row) or b in row:
+                        raise ValueError("supercell too small: cluster members alias onto the same site")
+                for mm in t.members[b]:
+                    offs.update(tuple(x) for x in (mm - _HCP_BASIS[b]).tolist())
+                col_set.update(x for row in idx for x in row)
+                d[t.name] = {
+                    "ref_indx": b,
+                    "size": t.size,
+                    "max_cluster_dia": cell.a * math.sqrt(t.dia2 / 108.0),
+                    "symm_group": b,
+                    "name": t.name,
+                    "descriptor": "hcp_%d_body_q_%d" % (t.size, t.dia2),
+                    "indices": idx,
+                    "order": [list(o) for o in t.orders[b]],
+                    "equiv_sites": [list(g) for g in t.equiv_sites],
+                }
+            sites = cell.index_of(np.array(sorted(offs), dtype=np.int64) + _HCP_BASIS[b])
+            if len(set(sites.tolist())) != len(sites):
+                raise ValueError("supercell too small: neighbour offsets alias onto the same site")
+            info.append(d)
+        self.cluster_info = info
+        cols = np.array(sorted(col_set), dtype=np.int64)
+        self.column_sites = cols
+        shift = cell.positions - cell.positions[basis_of]  # a lattice translation (same atom of the cell)
+        self.table = cell.index_of(cell.positions[cols][None, :, :] + shift[:, None, :]).astype(np.int32)
+        self._trans_list = None
+
+    trans_matrix = Settings.trans_matrix
+    symbol_ids = Settings.symbol_ids
+    bf_table = Settings.bf_table
+
+
+def hcp_settings(L: int, Lz: int, pair_shells: int, triplet_shells: int, quad_shells: int,
+                 symbols: Sequence[str], a: float = 3.21) -> HCPSettings:
+    """HCP supercell of ``L x L x Lz`` hexagonal cells (ideal c / a) with the given cluster recipe."""
+    return HCPSettings(HCPSupercell(L, Lz, a), enumerate_hcp_cluster_types(pair_shells, triplet_shells, quad_shells),
+                       symbols)

@@ -28,12 +28,14 @@ def load_golden(name):
 
 def settings_for(lattice, L, ps, ts, qs, syms):
     """``fcc``, ``l12`` or ``l12:<group of each sublattice>`` settings (the lattice key of a golden case)."""
-    from cemc_gb300.lattice import cubic_settings, fcc_settings, l12_settings
+    from cemc_gb300.lattice import cubic_settings, fcc_settings, hcp_settings, l12_settings
     if lattice.startswith("l12"):
         gob = tuple(int(ch) for ch in lattice.split(":")[1]) if ":" in lattice else (0, 1, 2, 3)
         return l12_settings(L, ps, ts, qs, syms, group_of_basis=gob)
     if lattice in ("bcc", "sc"):
         return cubic_settings(lattice, L, ps, ts, qs, syms)
+    if lattice.startswith("hcp"):  # hcp:<cells along c>
+        return hcp_settings(L, int(lattice.split(":")[1]), ps, ts, qs, syms)
     return fcc_settings(L, ps, ts, qs, syms)
 
 

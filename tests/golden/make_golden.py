@@ -35,7 +35,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from cemc_gb300.lattice import cubic_settings, fcc_settings, l12_settings, seeded_ecis, with_background  # noqa: E402
+from cemc_gb300.lattice import (cubic_settings, fcc_settings, hcp_settings, l12_settings, seeded_ecis,  # noqa: E402
+                                with_background)
 from cemc_gb300.tables import CEModel  # noqa: E402
 
 KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
@@ -44,7 +45,8 @@ KB = 8.6173303e-5  # eV/K, the constant of cpp/src/linear_vib_correction.cpp:3
 # background symbol (None: every site active; else an inert second sublattice of that species,
 # rocksalt-like, as in the reference's tests/test_sgc_mc.py:140-191), lattice ("fcc": one
 # translation-symmetry group; "l12": FCC under L1_2 symmetry, four groups, like the four-group
-# crystal of the reference's tests/helper_functions.py:8-27; "bcc", "sc": other cubic lattices)
+# crystal of the reference's tests/helper_functions.py:8-27; "bcc", "sc": other cubic lattices;
+# "hcp:<Lz>": L x L x Lz hexagonal close-packed cells)
 CASES = [
     ("binary_flip", 4, 4, 2, 1, ["Al", "Mg"], 0, 800.0, 3000, 11, None),
     ("binary_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 12, None),
@@ -62,6 +64,9 @@ CASES = [
     # other cubic Bravais lattices (the reference's tests use BCC and SC cells, test_CE_updater.py:21,206-228)
     ("bcc_swap", 4, 4, 2, 1, ["Al", "Mg"], 1, 800.0, 3000, 23, None, "bcc"),
     ("sc_ternary_flip", 5, 3, 2, 1, ["Al", "Mg", "Si"], 0, 800.0, 1500, 24, None, "sc"),
+    # HCP (space group P6_3/mmc): two translation groups related by a screw, 4 x 4 x 3 hexagonal cells
+    ("hcp_swap", 4, 3, 2, 1, ["Mg", "Zn"], 1, 800.0, 3000, 25, None, "hcp:3"),
+    ("hcp_ternary_flip", 4, 3, 2, 0, ["Al", "Mg", "Zn"], 0, 800.0, 1500, 26, None, "hcp:3"),
 ]
 
 
@@ -80,6 +85,8 @@ def make_settings(lattice, L, ps, ts, qs, syms):
         return l12_settings(L, ps, ts, qs, syms, group_of_basis=gob)
     if lattice in ("bcc", "sc"):
         return cubic_settings(lattice, L, ps, ts, qs, syms)
+    if lattice.startswith("hcp"):  # hcp:<cells along c>
+        return hcp_settings(L, int(lattice.split(":")[1]), ps, ts, qs, syms)
     return fcc_settings(L, ps, ts, qs, syms)
 
 

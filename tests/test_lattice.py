@@ -185,3 +185,26 @@ def test_l12_groups_share_names_and_pack_columns():
     merged = CEModel(l12_settings(4, 4, 2, 1, ["Al", "Mg"], group_of_basis=(0, 1, 1, 1)),
                      list(seeded_ecis(s.cset, 0)))
     assert merged.n_groups == 2 and np.allclose(merged.group_scale, [1.0, 1.0 / 3.0])
+
+
+def test_hcp_space_group_shells_and_groups():
+    """HCP (P6_3/mmc): 24 space-group operations, shells of 12, 6, 2, 18 neighbours, two translation groups
+    sharing every cluster name, in-plane and out-of-plane nearest-neighbour pairs as distinct types."""
+    from cemc_gb300.lattice import _HCP_BASIS, _hcp_ops, _hex_metric, hcp_settings, hcp_shell_radii
+    import itertools
+    assert len(_hcp_ops()) == 24
+    radii = hcp_shell_radii(4)
+    rng = np.arange(-3, 4)
+    cells = np.array(list(itertools.product(rng, rng, rng))) * 6
+    pts = (cells[:, None, :] + _HCP_BASIS[None]).reshape(-1, 3)
+    q = _hex_metric(pts)
+    assert [int((q == r).sum()) for r in radii] == [12, 6, 2, 18]
+    s = hcp_settings(4, 3, 3, 2, 1, ["Mg", "Zn"])
+    assert len(s.index_by_trans_symm) == 2 and set(s.cluster_info[0]) == set(s.cluster_info[1])
+    pairs = [t for t in s.cset.types if t.size == 2 and t.dia2 == 108]
+    assert sorted(len(t.members[0]) for t in pairs) == [6, 6]
+    m = CEModel(s, list(seeded_ecis(s.cset, 0)))
+    rows = [set(r.tolist()) for r in m.gpu_table]
+    for i in range(m.n_sites):
+        for j in rows[i]:
+            assert i in rows[j]
