@@ -240,7 +240,11 @@ class Montecarlo:
         raise NotImplementedError("bias potentials are not supported by the GPU drivers")
 
     def attach(self, obs, interval=1):
-        """Observers receive the final state at the end of runMC (per-step host callbacks would stall the GPU)."""
+        """Call ``obs(system_changes)`` every ``interval`` trials (montecarlo.py:403-415).
+
+        The trials between two observed steps run on the device as one launch, so a large
+        interval costs nothing; interval 1 turns every trial into its own launch.
+        """
         if not callable(obs):
             raise ValueError("The observer has to be a callable class!")
         self.observers.append((interval, obs))
@@ -262,7 +266,33 @@ class Montecarlo:
         return {m.symbols[i]: int(cnt[i]) for i in range(m.n_sym) if m.symbols[i] in self.symbols}
 
     def _run_trials(self, n: int, trace: bool = False):
-        """n trials through the fused kernel; drift reset every recompute_every_sweeps sweeps."""
+        """n trials through the fused kernel; drift reset every recompute_every_sweeps sweeps.
+
+        Attached observers are called like the reference's ``_mc_step`` calls them
+        (montecarlo.py:1031-1036): after every trial whose step number is a multiple of
+        the observer's interval, with that trial's changes (``(site, old, new)``, or
+        ``(site, old, old)`` when it was rejected).  The trials between two such steps
+        run as one launch; the observed trial runs alone, traced.
+        """
+        traces = []
+        done = 0
+        while done < n:
+            gap = self._steps_to_next_observation()
+            if gap is None or gap > n - done:
+                traces += self._run_block(n - done, trace)
+                break
+            if gap > 1:
+                traces += self._run_block(gap - 1, trace)
+            traces += self._observed_trial(trace)
+            done += gap
+        return traces
+
+    def _steps_to_next_observation(self):
+        """Trials until the next step at which an observer is due (None without observers)."""
+        gaps = [int(iv) - self.current_step % int(iv) for iv, _ in self.observers if int(iv) > 0]
+        return min(gaps) if gaps else None
+
+    def _run_block(self, n: int, trace: bool = False):
         ch = self.chain()
         m = self._calc().model
         block = self.recompute_every_sweeps * m.n_sites
@@ -279,6 +309,28 @@ class Montecarlo:
         self.current_step += n
         self._sync_after_run()
         return traces
+
+    def _observed_trial(self, trace: bool = False):
+        """One traced trial, then the observers due at this step get its changes."""
+        calc = self._calc()
+        syms = calc.model.symbols_of(calc.updater.occupation())
+        ch = self.chain()
+        tr = ch.run(1, precision=self.precision, warps=1, trace=True, **self._constraint_args())
+        self.current_step += 1
+        self._sync_after_run()
+        sites, acc, _ = (t.cpu().numpy() for t in tr)
+        a, b = int(sites[0, 0, 0]), int(sites[0, 0, 1])
+        accepted = bool(acc[0, 0])
+        if self.move == E.MOVE_SWAP:
+            sa, sb = syms[a], syms[b]
+            changes = [(a, sa, sb), (b, sb, sa)] if accepted else [(a, sa, sa), (b, sb, sb)]
+        else:
+            new = calc.model.symbols[b]
+            changes = [(a, syms[a], new)] if accepted else [(a, syms[a], syms[a])]
+        for interval, obs in self.observers:
+            if int(interval) > 0 and self.current_step % int(interval) == 0:
+                obs(changes)
+        return [tr] if trace else []
 
     def _warps(self):
         if self.warps:
@@ -312,12 +364,8 @@ class Montecarlo:
         self.current_energy = calc.get_energy()
 
     def _mc_step(self, verbose=False):
-        """One trial (the reference's _mc_step); returns (energy, accepted)."""
-        before = self.num_accepted
-        ch = self.chain()
-        _, acc, _ = ch.run(1, precision=self.precision, warps=1, trace=True, **self._constraint_args())
-        self.current_step += 1
-        self._sync_after_run()
+        """One trial (the reference's _mc_step, observers included); returns (energy, accepted)."""
+        (_, acc, _), = self._observed_trial(trace=True)
         return self.current_energy, bool(acc.cpu().numpy()[0, 0])
 
     def _probe_energy_bias(self, num_steps=1000):
@@ -479,8 +527,6 @@ class Montecarlo:
             self.log("Reached maximum number of steps ({} mc steps)".format(steps))
         self.elapsed = time.time() - start
         self._undo_energy_bias_from_eci()
-        for _, obs in self.observers:
-            obs([])
         return totalenergies
 
     # -- checkpoint / restart (montecarlo.py:1040-1074) ---------------------------------

@@ -453,3 +453,35 @@ def test_sgc_constraints_by_tag_and_fixed_element(torch_cuda):
         mc2.add_constraint(FixedElement(element=sym))
     with pytest.raises(CanNotFindLegalMoveError):
         mc2._run_trials(10)
+
+
+@pytest.mark.parametrize("sgc", [False, True])
+def test_observers_called_at_their_interval(sgc, torch_cuda):
+    """Observers run every `interval` trials with that trial's changes (montecarlo.py:1031-1036): the
+    swap / flip tuples, no-op tuples after a rejection, and the atoms already showing the new symbols."""
+    from cemc_gb300.mcmc import Montecarlo, SGCMonteCarlo
+    atoms, calc, s, eci = _calc()
+    mc = SGCMonteCarlo(atoms, 900.0, seed=3) if sgc else Montecarlo(atoms, 900.0, seed=3)
+    calls = []
+
+    class Obs:
+        def __call__(self, changes):
+            calls.append((mc.current_step, list(changes), [atoms[c[0]].symbol for c in changes],
+                          calc.get_energy()))
+
+    mc.attach(Obs(), interval=250)
+    if sgc:
+        mc.runMC(steps=2000, chem_potential={"c1_0": 0.02}, equil=False)
+    else:
+        mc.runMC(steps=2000, equil=False)
+    assert len(calls) == 12  # 4 during the 1000-trial bias probe, 8 in the main loop
+    n_changed = 0
+    for step, changes, now, energy in calls:
+        assert step % 250 == 0 and len(changes) == (1 if sgc else 2)
+        for (site, old, new), cur in zip(changes, now):
+            assert cur == new
+            n_changed += old != new
+        if not sgc:
+            (a, sa, sb), (b, sb2, sa2) = changes
+            assert (sa, sb) == (sa2, sb2) or (sa == sb and sa2 == sb2)
+    assert n_changed > 0
