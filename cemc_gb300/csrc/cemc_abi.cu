@@ -534,7 +534,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
     return fail(CEMC_ERR_LIMIT, "the table kernel needs translation groups of equal size and pattern tables of at "
                                 "most %d entries", cemc::kMaxTable);
   // move constraints are checked (and redrawn) by the one-trial-per-warp forms
-  const bool constrained = r->site_allow != nullptr || r->frozen != nullptr;
+  const bool constrained = r->site_allow != nullptr || r->frozen != nullptr || r->accept_first != 0;
   if (r->max_attempts < 0) return fail(CEMC_ERR_ARG, "max_attempts must be >= 0");
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP && !constrained;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
@@ -583,6 +583,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   a.site_allow = r->site_allow;
   a.frozen = r->frozen;
   a.max_attempts = r->max_attempts > 0 ? r->max_attempts : 10000;
+  a.accept_first = r->accept_first != 0;
   a.tpw = tpw;
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
   // Evaluation forms to try, in order: spin, or table then generic (AUTO), or the one asked for.

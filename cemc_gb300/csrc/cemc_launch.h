@@ -36,6 +36,7 @@ struct RunArgs {
   const uint8_t *site_allow;  // move constraints (see cemc_run_desc), NULL = none
   const uint32_t *frozen;
   int max_attempts;
+  int accept_first;  // the first trial of the call (chunk offset 0) is accepted whatever its energy change
 };
 
 constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two or three more warps are helpers

@@ -987,7 +987,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           }
           int acc = 0;
           if (lane == 0) {
-            acc = no_move ? 0 : metropolis<R>(de, ua, ub, kT, inv_kT);
+            // accept_first_trial_move_after_reset: the call's first trial is accepted outright
+            const bool first = TPW == 1 && a.accept_first && a.chunk_offset == 0 && t == t_first;
+            acc = no_move ? 0 : (first ? 1 : metropolis<R>(de, ua, ub, kT, inv_kT));
             if (no_move) put(&misc[3], 1);  // reported in the status at the end of the launch
             put(&r_sa[gidx], (int32_t)sa);
             put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));

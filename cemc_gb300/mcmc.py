@@ -75,8 +75,10 @@ class Montecarlo:
         self.min_acc_rate = min_acc_rate
         if recycle_waste:
             raise NotImplementedError("waste recycling is not supported by the GPU drivers")
-        if accept_first_trial_move_after_reset:
-            raise NotImplementedError("accept_first_trial_move_after_reset is not supported by the GPU drivers")
+        # the next trial is accepted outright after construction, reset() and set_symbols()
+        # (montecarlo.py:128-131, 294-295, 363-364, 932-935)
+        self.accept_first_trial_move_after_reset = bool(accept_first_trial_move_after_reset)
+        self.is_first = self.accept_first_trial_move_after_reset
         if max_constraint_attempts <= 0:
             raise ValueError("Max. constraint attempts has to be > 0!")
         self.recycle_waste = False
@@ -155,6 +157,8 @@ class Montecarlo:
         self._invalidate_chain()
         self.symbols = sorted(set(symbs))
         self.update_current_energy()
+        if self.accept_first_trial_move_after_reset:
+            self.is_first = True
 
     def add_constraint(self, constraint):
         """Add a move constraint (montecarlo.py:386-392), enforced on the device.
@@ -175,6 +179,13 @@ class Montecarlo:
             if not constraint(system_changes):
                 return False
         return True
+
+    def _first_arg(self):
+        """``accept_first`` for the next launch: consumes the pending first-trial acceptance."""
+        if getattr(self, "is_first", False):
+            self.is_first = False
+            return {"accept_first": True}
+        return {}
 
     def _constraint_args(self):
         """Device masks and redraw limit of the constraints, as ``ChainBatch.run`` arguments."""
@@ -256,6 +267,8 @@ class Montecarlo:
                 obs.reset()
         self.current_step = 0
         self.num_accepted = 0
+        if self.accept_first_trial_move_after_reset:
+            self.is_first = True
         ch = self.chain()
         ch.reset_accumulators()
 
@@ -300,7 +313,8 @@ class Montecarlo:
         done = 0
         while done < n:
             k = min(block, n - done)
-            tr = ch.run(k, precision=self.precision, warps=self._warps(), trace=trace, **self._constraint_args())
+            tr = ch.run(k, precision=self.precision, warps=self._warps(), trace=trace, **self._constraint_args(),
+                        **self._first_arg())
             if trace:
                 traces.append(tr)
             if k == block:
@@ -315,7 +329,7 @@ class Montecarlo:
         calc = self._calc()
         syms = calc.model.symbols_of(calc.updater.occupation())
         ch = self.chain()
-        tr = ch.run(1, precision=self.precision, warps=1, trace=True, **self._constraint_args())
+        tr = ch.run(1, precision=self.precision, warps=1, trace=True, **self._constraint_args(), **self._first_arg())
         self.current_step += 1
         self._sync_after_run()
         sites, acc, _ = (t.cpu().numpy() for t in tr)
@@ -532,7 +546,8 @@ class Montecarlo:
     # -- checkpoint / restart (montecarlo.py:1040-1074) ---------------------------------
     _CHECKPOINT_ATTRS = ("T", "min_acc_rate", "current_step", "num_accepted", "status_every_sec", "energy_bias",
                          "correlation_info", "precision", "warps", "recompute_every_sweeps", "seed", "symbols",
-                         "current_energy", "logfile", "name", "max_allowed_constraint_pass_attempts")
+                         "current_energy", "logfile", "name", "max_allowed_constraint_pass_attempts",
+                         "accept_first_trial_move_after_reset", "is_first")
 
     def _checkpoint_attrs(self):
         return self._CHECKPOINT_ATTRS

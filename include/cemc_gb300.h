@@ -176,6 +176,8 @@ typedef struct {
   const uint8_t *site_allow;    /* [n_chains * n_sites] bit s: species s may be placed on the site, or NULL */
   const uint32_t *frozen;       /* [n_chains] bit s: a site holding species s may not change, or NULL */
   int32_t max_attempts;         /* redraws per trial; 0 = 10000 (the reference's default) */
+  int32_t accept_first;         /* 1: the first trial of this call is accepted whatever its energy change
+                                   (accept_first_trial_move_after_reset, montecarlo.py:932-935) */
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when

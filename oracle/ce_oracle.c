@@ -279,6 +279,8 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
     if (no_move) {
       accept = 0;
       rc = ORC_ERR_NO_MOVE;
+    } else if (c->accept_first && it == 0) {
+      accept = 1;
     } else if (e_new < e_cur) {
       accept = 1;
     } else {

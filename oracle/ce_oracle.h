@@ -51,6 +51,7 @@ typedef struct {
   const uint8_t *allow;
   uint32_t frozen;
   int32_t max_attempts;
+  int32_t accept_first; /* 1: the run's first trial is accepted outright (montecarlo.py:932-935) */
 } orc_chain;
 
 typedef struct {

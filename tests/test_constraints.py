@@ -134,3 +134,25 @@ def test_oracle_reports_exhausted_redraws(oracle_mod):
         orc.run(st, seed=1, chain_id=0, t_begin=0, n_trials=20, trace=True)
     assert not ei.value.trace.acc.any()
     assert np.array_equal(st.occ, occ)
+
+
+def test_oracle_accepts_the_first_trial_when_asked(oracle_mod):
+    """accept_first_trial_move_after_reset (montecarlo.py:932-935): the run's first trial is accepted
+    whatever its energy change; the rest follow Metropolis."""
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(4, 3, 2, 0, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    orc = oracle_mod.Oracle(m)
+    occ = np.random.default_rng(8).integers(0, 2, m.n_sites).astype(np.int8)
+    for seed in range(50):  # a stream whose first proposal raises the energy
+        plain = orc.new_chain_state(occ, m.eci_vector(eci), KB * 5.0, 1)
+        tr0 = orc.run(plain, seed=seed, chain_id=0, t_begin=0, n_trials=50, trace=True)
+        if tr0.de[0] > 0:
+            break
+    assert tr0.de[0] > 0 and tr0.acc[0] == 0
+    first = orc.new_chain_state(occ, m.eci_vector(eci), KB * 5.0, 1, accept_first=1)
+    tr1 = orc.run(first, seed=seed, chain_id=0, t_begin=0, n_trials=50, trace=True)
+    assert tr1.acc[0] == 1 and tr1.de[0] == tr0.de[0]
+    assert np.array_equal(tr0.site[:2], tr1.site[:2])

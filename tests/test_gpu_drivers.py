@@ -485,3 +485,18 @@ def test_observers_called_at_their_interval(sgc, torch_cuda):
             (a, sa, sb), (b, sb2, sa2) = changes
             assert (sa, sb) == (sa2, sb2) or (sa == sb and sa2 == sb2)
     assert n_changed > 0
+
+
+def test_accept_first_trial_move_after_reset(torch_cuda):
+    """montecarlo.py:128-131, 363-364, 932-935: after construction and after every reset the next trial is
+    accepted whatever its energy change."""
+    from cemc_gb300.mcmc import Montecarlo
+    atoms, calc, s, eci = _calc()
+    mc = Montecarlo(atoms, 1.0, seed=2, accept_first_trial_move_after_reset=True)
+    for _ in range(3):
+        e0 = mc.current_energy
+        _, accepted = mc._mc_step()
+        assert accepted
+        mc.reset()
+    mc2 = Montecarlo(atoms, 1.0, seed=2)
+    assert sum(mc2._mc_step()[1] for _ in range(5)) <= 5

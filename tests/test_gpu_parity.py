@@ -507,3 +507,27 @@ def test_gpu_constraints_without_legal_move_report_status(kernel, E, oracle_mod)
     st = oracle_mod.Oracle(m).new_chain_state(occ[0], g["eci"], float(g["kT"]), 1, frozen=0b01, max_attempts=7)
     with pytest.raises(oracle_mod.NoLegalMove):
         oracle_mod.Oracle(m).run(st, seed=3, chain_id=0, t_begin=0, n_trials=50)
+
+
+@pytest.mark.parametrize("kernel", [1, 2, 4])
+@pytest.mark.parametrize("move", [0, 1])
+def test_gpu_accept_first_matches_oracle(move, kernel, E, oracle_mod):
+    """The call's first trial is accepted outright on every chain (accept_first_trial_move_after_reset),
+    at a temperature where it would be rejected; the chains then equal the oracle's."""
+    g = load_golden("binary_flip")
+    s, m, eci = golden_model(g)
+    _kernel_ok(m, kernel, E, move)
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(21)
+    occ = rng.integers(0, 2, (3, m.n_sites)).astype(np.int8)
+    keys = [1, 4, 9]
+    cb = E.ChainBatch(geo, occ, g["eci"], KB * 20.0, move, seed=6, chain_keys=keys)
+    _, acc, _ = cb.run(400, precision=E.PREC_F64, warps=8, trace=True, kernel=kernel, accept_first=True)
+    _sync()
+    acc = acc.cpu().numpy()
+    for c in range(3):
+        st = oracle_mod.Oracle(m).new_chain_state(occ[c], g["eci"], KB * 20.0, move, accept_first=1)
+        tr = oracle_mod.Oracle(m).run(st, seed=6, chain_id=keys[c], t_begin=0, n_trials=400, trace=True)
+        assert acc[c, 0] == 1 and np.array_equal(acc[c], tr.acc)
+        assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
+        assert _cf_close(cb.cf.cpu().numpy()[c], st.cf)
