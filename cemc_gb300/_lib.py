@@ -63,7 +63,7 @@ class RunDesc(C.Structure):
                 ("accum_slot", _P), ("chain_trials", _P), ("kernel", C.c_int32), ("cluster", C.c_int32),
                 ("scratch", _P), ("scratch_doubles", C.c_uint64), ("stamps", _P), ("stamp_words", C.c_uint64),
                 ("kernel_used", C.c_int32), ("site_allow", _P), ("frozen", _P), ("max_attempts", C.c_int32),
-                ("accept_first", C.c_int32)]
+                ("accept_first", C.c_int32), ("recycle_waste", C.c_int32)]
 
 
 class CemcError(RuntimeError):

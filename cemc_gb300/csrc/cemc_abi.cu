@@ -525,16 +525,21 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_TABLE)
     return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
   if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
+  // waste recycling runs its own build of the generic form, one CTA per chain
+  const bool recycle = r->recycle_waste != 0;
+  if (recycle && r->kernel != CEMC_KERNEL_AUTO && r->kernel != CEMC_KERNEL_GENERIC)
+    return fail(CEMC_ERR_ARG, "waste recycling runs the generic kernel form");
+  if (recycle && r->cluster == 2) return fail(CEMC_ERR_ARG, "waste recycling runs one CTA per chain");
   const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
   if (want_spin && !geo->spin_ok)
     return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1, <= 64 columns and "
                               "one translation-symmetry group");
-  const bool use_spin = want_spin || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok);
+  const bool use_spin = want_spin || (r->kernel == CEMC_KERNEL_AUTO && geo->spin_ok && !recycle);
   if (r->kernel == CEMC_KERNEL_TABLE && !g.table_ok)
     return fail(CEMC_ERR_LIMIT, "the table kernel needs translation groups of equal size and pattern tables of at "
                                 "most %d entries", cemc::kMaxTable);
   // move constraints are checked (and redrawn) by the one-trial-per-warp forms
-  const bool constrained = r->site_allow != nullptr || r->frozen != nullptr || r->accept_first != 0;
+  const bool constrained = r->site_allow != nullptr || r->frozen != nullptr || r->accept_first != 0 || recycle;
   if (r->max_attempts < 0) return fail(CEMC_ERR_ARG, "max_attempts must be >= 0");
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP && !constrained;
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
@@ -588,7 +593,9 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
   // Evaluation forms to try, in order: spin, or table then generic (AUTO), or the one asked for.
   std::vector<int> forms;
-  if (use_spin)
+  if (recycle)
+    forms = {cemc::kFormRecycle};
+  else if (use_spin)
     forms = {cemc::kFormSpin};
   else if (r->kernel == CEMC_KERNEL_TABLE)
     forms = {cemc::kFormTable};
@@ -650,7 +657,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   bool found = false;
   for (size_t fi = 0; fi < forms.size() && !found; ++fi) {
     form = forms[fi];
-    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && 2 * r->n_chains <= geo->n_sms &&
+    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && !recycle && 2 * r->n_chains <= geo->n_sms &&
                             (round_cap == 0 || round_cap >= 2 * warps))) {
       cemc::RunArgs x = a;
       cemc::McLayout L2{};
@@ -697,7 +704,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
     done += n;
   }
   r->kernel_used = form == cemc::kFormTable ? CEMC_KERNEL_TABLE
-                  : form == cemc::kFormGeneric ? CEMC_KERNEL_GENERIC
+                  : (form == cemc::kFormGeneric || form == cemc::kFormRecycle) ? CEMC_KERNEL_GENERIC
                   : (a.tpw == 2 ? CEMC_KERNEL_SPIN_HALFWARP : CEMC_KERNEL_SPIN);
   if (form == cemc::kFormTable) {
     cudaError_t e = cemc::launch_recompute(g, r->n_chains, r->occ, r->eci, r->cf, r->energy, rscratch,

@@ -169,6 +169,16 @@ __device__ __forceinline__ int metropolis(R de, uint32_t ua, uint32_t ub, double
   return cemc_u01_53(ua, ub) <= exp(-(double)de / kT);
 }
 
+// Two-state acceptance of waste recycling (Frenkel, PNAS 101, 17571 (2004);
+// montecarlo.py:937-948): the reference draws the next state from the weights
+// exp(-E / kT) of the current and the proposed state, i.e. it accepts when
+// u > p0 = 1 / (1 + exp(-dE / kT)), evaluated here in FP64.
+template <typename R>
+__device__ __forceinline__ int barker(R de, uint32_t ua, uint32_t ub, double kT) {
+  const double p0 = 1.0 / (1.0 + exp(-(double)de / kT));
+  return cemc_u01_53(ua, ub) > p0;
+}
+
 // Fill one warp's vals array for a change of `site` from species `old_s` to
 // `new_s`.  Neighbour species come from `occ`, except that `ovr_site` (if >=
 // 0) is read as species `ovr_s` (the first half of a swap already applied).

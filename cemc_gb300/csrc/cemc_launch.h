@@ -84,6 +84,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t
 constexpr int kFormGeneric = 0;  // basis-function products term by term; tracks correlation functions
 constexpr int kFormSpin = 1;     // binary +1/-1 basis: bit-packed neighbourhoods
 constexpr int kFormTable = 2;    // one lookup per cluster geometry; correlation functions by a final recompute
+constexpr int kFormRecycle = 3;  // the generic evaluation with waste-recycled acceptance and running sums
 
 __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int move, int rsize, int occ_smem,
                                               int trk_smem, int stamp_bits, int n_cl, int n_masks, int ring_bits,

@@ -234,6 +234,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
   constexpr bool SPIN = (FORM == kFormSpin), TAB = (FORM == kFormTable);
+  constexpr bool RECYCLE = (FORM == kFormRecycle);  // generic evaluation, waste-recycled acceptance and sums
   const int W = a.warps;   // evaluating warps per CTA, then NB booker warps and one fetcher warp
   const int CW = round_trials(CL, W, TPW);  // trials per round
   const int NB = n_bookers(CL, W, TPW);
@@ -550,7 +551,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         }
       }
     }
-    if (mine) {
+    if (mine && !RECYCLE) {
       const A ve = acc_add_x(eoff, x);
       lacc[lane] = acc_add(lacc[lane], ve);
       lacc[32 + lane] = acc_add(lacc[32 + lane], acc_mul(ve, ve));
@@ -562,6 +563,38 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           l[0] = acc_add(l[0], vs);
           l[CEMC_MAX_BF * 32] = acc_add(l[CEMC_MAX_BF * 32], acc_mul(vs, vs));
           l[2 * CEMC_MAX_BF * 32] = acc_add(l[2 * CEMC_MAX_BF * 32], acc_mul(vs, ve));
+        }
+      }
+    }
+    if constexpr (RECYCLE) {
+      // Waste recycling (mc_observers.py:231-258, montecarlo.py:805-809): every trial adds
+      // p0 x (value before it) + p1 x (value of its proposal), p1 = 1 / (1 + exp(dE / kT)).
+      // The energies are those of the state before and of the proposed state; the singlets
+      // are the calculator's before and after the step (after a rejection both are the
+      // state before, as the reference's observer reads them).
+      if (mine) {
+        const R dE = r_de[gg];
+        const double p1d = 1.0 / (1.0 + exp((double)dE / kT));
+        const A P1 = acc_from<A>(p1d), P0 = acc_from<A>(1.0 - p1d);
+        const A e_after = acc_add_x(eoff, x);
+        const A e_before = acc ? acc_add_x(e_after, -dE) : e_after;
+        const A e_prop = acc_add_x(e_before, dE);
+        lacc[lane] = acc_add(lacc[lane], acc_add(acc_mul(P0, e_before), acc_mul(P1, e_prop)));
+        lacc[32 + lane] = acc_add(lacc[32 + lane], acc_add(acc_mul(P0, acc_mul(e_before, e_before)),
+                                                           acc_mul(P1, acc_mul(e_prop, e_prop))));
+#pragma unroll
+        for (int b = 0; b < NBF; ++b) {
+          if (b < g.n_bf) {
+            const R own = acc ? r_ds[b * kRoundSlots + gg] : (R)0;
+            const A s_after = acc_add(s_start[b], acc_mul(acc_add_x(dsum[b], ds[b]), s_start[CEMC_MAX_BF]));
+            const A s_before = acc_add(s_start[b], acc_mul(acc_add_x(dsum[b], ds[b] - own), s_start[CEMC_MAX_BF]));
+            A *l = lacc + (2 + b) * 32 + lane;
+            l[0] = acc_add(l[0], acc_add(acc_mul(P0, s_before), acc_mul(P1, s_after)));
+            l[CEMC_MAX_BF * 32] = acc_add(l[CEMC_MAX_BF * 32], acc_add(acc_mul(P0, acc_mul(s_before, s_before)),
+                                                                     acc_mul(P1, acc_mul(s_after, s_after))));
+            l[2 * CEMC_MAX_BF * 32] = acc_add(l[2 * CEMC_MAX_BF * 32], acc_add(acc_mul(P0, acc_mul(s_before, e_before)),
+                                                                             acc_mul(P1, acc_mul(s_after, e_prop))));
+          }
         }
       }
     }
@@ -989,7 +1022,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           if (lane == 0) {
             // accept_first_trial_move_after_reset: the call's first trial is accepted outright
             const bool first = TPW == 1 && a.accept_first && a.chunk_offset == 0 && t == t_first;
-            acc = no_move ? 0 : (first ? 1 : metropolis<R>(de, ua, ub, kT, inv_kT));
+            if constexpr (RECYCLE)
+              acc = no_move ? 0 : (first ? 1 : barker<R>(de, ua, ub, kT));
+            else
+              acc = no_move ? 0 : (first ? 1 : metropolis<R>(de, ua, ub, kT, inv_kT));
             if (no_move) put(&misc[3], 1);  // reported in the status at the end of the launch
             put(&r_sa[gidx], (int32_t)sa);
             put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
@@ -1251,11 +1287,23 @@ static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t 
   return launch_f<R, CEMC_MOVE_FLIP, kFormGeneric>(g, a, smem, st, none);
 }
 
+template <typename R>
+static cudaError_t launch_recycle(const DevGeo &g, const RunArgs &a, int move, size_t smem, cudaStream_t st) {
+  const SpinDev none{};
+  return move == CEMC_MOVE_SWAP ? launch_t<R, CEMC_MOVE_SWAP, kFormRecycle, 1, 1>(g, a, smem, st, none)
+                                : launch_t<R, CEMC_MOVE_FLIP, kFormRecycle, 1, 1>(g, a, smem, st, none);
+}
+
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       int form, const SpinDev *spin) {
   // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
   if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP)) return cudaErrorInvalidValue;
   if (form == kFormSpin && !spin) return cudaErrorInvalidValue;
+  if (form == kFormRecycle) {
+    if (a.cl != 1 || a.tpw != 1) return cudaErrorInvalidValue;
+    return precision == CEMC_PREC_F32 ? launch_recycle<float>(g, a, move, smem, st)
+                                      : launch_recycle<double>(g, a, move, smem, st);
+  }
   return precision == CEMC_PREC_F32 ? launch_r<float>(g, a, move, smem, st, form, spin)
                                     : launch_r<double>(g, a, move, smem, st, form, spin);
 }

@@ -293,7 +293,7 @@ class ChainBatch:
     def run(self, n_trials: int, precision: int = PREC_F64, warps: int = 0, trace: bool = False,
             chain_trials: Optional[torch.Tensor] = None, kernel: int = 0, cluster: int = 0,
             site_allow: Optional[torch.Tensor] = None, frozen: Optional[torch.Tensor] = None,
-            max_attempts: int = 0, accept_first: bool = False):
+            max_attempts: int = 0, accept_first: bool = False, recycle_waste: bool = False):
         """Run ``n_trials`` trials on every chain in one launch (``cemc_run``).
 
         ``chain_trials`` (device int64, one per chain, each <= n_trials) gives chains their own counts.
@@ -302,6 +302,7 @@ class ChainBatch:
         placed on the site), ``frozen`` (device int32 [n_chains], bit s = a site holding species s may
         not change), ``max_attempts`` redraws per trial (0 = 10000); see ``mc_constraints``.
         ``accept_first``: the first trial of the call is accepted outright (every chain).
+        ``recycle_waste``: waste-recycled acceptance and running sums (generic form, one CTA).
         """
         if site_allow is not None:
             if site_allow.dtype != torch.uint8 or site_allow.numel() != self.n_chains * self.geo.model.n_sites:
@@ -321,7 +322,8 @@ class ChainBatch:
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
                          _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel(),
                          _ptr(self._stamps()), self._stamp_buf.numel() if self._stamp_buf is not None else 0,
-                         0, _ptr(site_allow), _ptr(frozen), int(max_attempts), int(bool(accept_first)))
+                         0, _ptr(site_allow), _ptr(frozen), int(max_attempts), int(bool(accept_first)),
+                         int(bool(recycle_waste)))
         with torch.cuda.device(self.occ.device):
             _lib.check(self.geo.L.cemc_run(self.geo.handle, C.byref(d), _stream_ptr(self.stream)))
         # the table form ends the call with a full recompute (cf and energy exact already)

@@ -73,15 +73,14 @@ class Montecarlo:
         self.atoms = atoms
         self.T = float(temp)
         self.min_acc_rate = min_acc_rate
-        if recycle_waste:
-            raise NotImplementedError("waste recycling is not supported by the GPU drivers")
+        # waste recycling (montecarlo.py:937-948): two-state acceptance and weighted sums on the device
+        self.recycle_waste = bool(recycle_waste)
         # the next trial is accepted outright after construction, reset() and set_symbols()
         # (montecarlo.py:128-131, 294-295, 363-364, 932-935)
         self.accept_first_trial_move_after_reset = bool(accept_first_trial_move_after_reset)
         self.is_first = self.accept_first_trial_move_after_reset
         if max_constraint_attempts <= 0:
             raise ValueError("Max. constraint attempts has to be > 0!")
-        self.recycle_waste = False
         self.indeces = range(len(atoms)) if indeces is None else indeces
         self.observers = []
         self.constraints = []
@@ -181,11 +180,13 @@ class Montecarlo:
         return True
 
     def _first_arg(self):
-        """``accept_first`` for the next launch: consumes the pending first-trial acceptance."""
+        """Per-launch flags: waste recycling, and ``accept_first`` (consumes the pending first-trial
+        acceptance)."""
+        out = {"recycle_waste": True} if self.recycle_waste else {}
         if getattr(self, "is_first", False):
             self.is_first = False
-            return {"accept_first": True}
-        return {}
+            out["accept_first"] = True
+        return out
 
     def _constraint_args(self):
         """Device masks and redraw limit of the constraints, as ``ChainBatch.run`` arguments."""
@@ -547,7 +548,7 @@ class Montecarlo:
     _CHECKPOINT_ATTRS = ("T", "min_acc_rate", "current_step", "num_accepted", "status_every_sec", "energy_bias",
                          "correlation_info", "precision", "warps", "recompute_every_sweeps", "seed", "symbols",
                          "current_energy", "logfile", "name", "max_allowed_constraint_pass_attempts",
-                         "accept_first_trial_move_after_reset", "is_first")
+                         "accept_first_trial_move_after_reset", "is_first", "recycle_waste")
 
     def _checkpoint_attrs(self):
         return self._CHECKPOINT_ATTRS

@@ -178,6 +178,9 @@ typedef struct {
   int32_t max_attempts;         /* redraws per trial; 0 = 10000 (the reference's default) */
   int32_t accept_first;         /* 1: the first trial of this call is accepted whatever its energy change
                                    (accept_first_trial_move_after_reset, montecarlo.py:932-935) */
+  int32_t recycle_waste;        /* 1: waste recycling (Frenkel 2004; montecarlo.py:937-948): accept when
+                                   u > 1 / (1 + exp(-dE / kT)), and every trial adds p0 x (value before) +
+                                   p1 x (value of the proposal) to the running sums; generic form, one CTA */
 } cemc_run_desc;
 
 /* Kernel selection of cemc_run.  AUTO takes the binary spin-basis form when

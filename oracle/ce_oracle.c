@@ -181,6 +181,26 @@ static int change_legal(const orc_chain *c, int site, int old_s, int new_s) {
   return 1;
 }
 
+/* Waste recycling (Frenkel 2004): every trial adds p0 x (value before) + p1 x (value of the
+ * proposal), p1 = 1 / (1 + exp(dE / kT)); energies of the state before and of the proposed
+ * state (montecarlo.py:805-809), singlets as the calculator reports them before and after the
+ * step, i.e. unchanged after a rejection (mc_observers.py:231-258). */
+static void accumulate_recycled(const orc_model *m, const double *cf_before, const double *cf_after, double e_before,
+                                double e_prop, double p1, cemc_accum *acc) {
+  if (!acc) return;
+  const double p0 = 1.0 - p1;
+  const double db = e_before - acc->e_ref, dp = e_prop - acc->e_ref;
+  acc->sum_e += p0 * db + p1 * dp;
+  acc->sum_e2 += p0 * db * db + p1 * dp * dp;
+  for (int b = 0; b < m->n_bf; ++b) {
+    const double sb = cf_before[m->singlet_eci[b]], sa = cf_after[m->singlet_eci[b]];
+    acc->sum_s[b] += p0 * sb + p1 * sa;
+    acc->sum_s2[b] += p0 * sb * sb + p1 * sa * sa;
+    acc->sum_se[b] += p0 * sb * db + p1 * sa * dp;
+  }
+  acc->n_samples++;
+}
+
 static void accumulate(const orc_model *m, const double *cf, double e, cemc_accum *acc) {
   if (!acc) return;
   const double de = e - acc->e_ref;
@@ -200,9 +220,11 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
   const int n_eci = m->n_eci;
   double *next = (double *)malloc(sizeof(double) * n_eci);
   double *next2 = (double *)malloc(sizeof(double) * n_eci);
-  if (!next || !next2) {
+  double *cf_before = (double *)malloc(sizeof(double) * n_eci); /* waste recycling: singlets before a trial */
+  if (!next || !next2 || !cf_before) {
     free(next);
     free(next2);
+    free(cf_before);
     return ORC_ERR_ARG;
   }
   int present[ORC_MAX_SYM];
@@ -213,6 +235,7 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
     if (n_present < 2) {
       free(next);
       free(next2);
+      free(cf_before);
       return ORC_ERR_STATE;
     }
   }
@@ -281,12 +304,17 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
       rc = ORC_ERR_NO_MOVE;
     } else if (c->accept_first && it == 0) {
       accept = 1;
+    } else if (c->recycle) {
+      /* the next state drawn from the weights of the current and the proposed state */
+      accept = u > 1.0 / (1.0 + exp(-(e_new - e_cur) / c->kT));
     } else if (e_new < e_cur) {
       accept = 1;
     } else {
       const double prob = exp(-(e_new - e_cur) / c->kT);
       accept = (u <= prob);
     }
+    const double e_before = e_cur;
+    if (c->recycle) memcpy(cf_before, c->cf, sizeof(double) * n_eci);
     if (trace) {
       trace->site[2 * it] = a;
       trace->site[2 * it + 1] = (move == ORC_MOVE_FLIP) ? na : b;
@@ -311,11 +339,16 @@ int orc_run_chain(const orc_model *m, orc_chain *c, int move, uint64_t seed, uin
       }
       if (c->acc) c->acc->n_accept++;
     }
-    accumulate(m, c->cf, e_cur, c->acc);
+    if (c->recycle)
+      accumulate_recycled(m, cf_before, c->cf, e_before, e_new, 1.0 / (1.0 + exp((e_new - e_before) / c->kT)),
+                          c->acc);
+    else
+      accumulate(m, c->cf, e_cur, c->acc);
   }
   *c->energy = e_cur;
   free(next);
   free(next2);
+  free(cf_before);
   return rc;
 }
 

@@ -52,6 +52,7 @@ typedef struct {
   uint32_t frozen;
   int32_t max_attempts;
   int32_t accept_first; /* 1: the run's first trial is accepted outright (montecarlo.py:932-935) */
+  int32_t recycle;      /* 1: waste recycling (montecarlo.py:937-948, mc_observers.py:231-258) */
 } orc_chain;
 
 typedef struct {

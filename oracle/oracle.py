@@ -49,7 +49,8 @@ class OrcModel(C.Structure):
 class OrcChain(C.Structure):
     _fields_ = [("occ", _P), ("cf", _P), ("eci", _P), ("kT", C.c_double), ("energy", _P), ("acc", _P),
                 ("trk", _P), ("loc", _P), ("trk_start", _P), ("trk_count", _P),
-                ("allow", _P), ("frozen", C.c_uint32), ("max_attempts", C.c_int32), ("accept_first", C.c_int32)]
+                ("allow", _P), ("frozen", C.c_uint32), ("max_attempts", C.c_int32), ("accept_first", C.c_int32),
+                ("recycle", C.c_int32)]
 
 
 class NoLegalMove(RuntimeError):
@@ -158,7 +159,7 @@ class Oracle:
 
     def new_chain_state(self, occ: np.ndarray, eci: np.ndarray, kT: float, move: int, e_ref: Optional[float] = None,
                         allow: Optional[np.ndarray] = None, frozen: int = 0, max_attempts: int = 0,
-                        accept_first: int = 0):
+                        accept_first: int = 0, recycle: int = 0):
         """Host-side chain (occ, cf from the full recompute, energy, tracker, sums).
 
         ``allow`` (uint8 per site, bit s = species s may be placed there), ``frozen`` (bit s = a site
@@ -184,13 +185,15 @@ class Oracle:
         st.frozen = int(frozen)
         st.max_attempts = int(max_attempts)
         st.accept_first = int(accept_first)
+        st.recycle = int(recycle)
         return st
 
     def _cchain(self, st) -> OrcChain:
         return OrcChain(_ptr(st.occ), _ptr(st.cf), _ptr(st.eci), st.kT, _ptr(st.energy), _ptr(st.acc),
                         _ptr(st.trk), _ptr(st.loc), _ptr(st.trk_start), _ptr(st.trk_count),
                         _ptr(getattr(st, "allow", None)), int(getattr(st, "frozen", 0)),
-                        int(getattr(st, "max_attempts", 0)), int(getattr(st, "accept_first", 0)))
+                        int(getattr(st, "max_attempts", 0)), int(getattr(st, "accept_first", 0)),
+                        int(getattr(st, "recycle", 0)))
 
     def run(self, st, seed: int, chain_id: int, t_begin: int, n_trials: int, trace: bool = False):
         """Run trials [t_begin, t_begin + n_trials) of one chain in place; optional per-trial trace."""

@@ -156,3 +156,57 @@ def test_oracle_accepts_the_first_trial_when_asked(oracle_mod):
     tr1 = orc.run(first, seed=seed, chain_id=0, t_begin=0, n_trials=50, trace=True)
     assert tr1.acc[0] == 1 and tr1.de[0] == tr0.de[0]
     assert np.array_equal(tr0.site[:2], tr1.site[:2])
+
+
+@pytest.mark.parametrize("move", [0, 1])
+def test_oracle_waste_recycling_follows_the_reference(move, oracle_mod):
+    """Waste recycling (montecarlo.py:937-948, util.py:41-63, mc_observers.py:231-258): acceptance
+    u > w0 / (w0 + w1) with w = exp(-(E - min E) / kT) over (current, proposed); every trial adds
+    w-weighted energies of the current and proposed states and the calculator's singlets before and
+    after the step.  Replayed here from the trace with the reference's own formulas."""
+    from cemc_gb300.lattice import fcc_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    s = fcc_settings(4, 3, 2, 0, ["Al", "Mg"])
+    eci = seeded_ecis(s.cset, 0)
+    m = CEModel(s, list(eci))
+    orc = oracle_mod.Oracle(m)
+    occ = np.random.default_rng(2).integers(0, 2, m.n_sites).astype(np.int8)
+    kT = KB * 700.0
+    st = orc.new_chain_state(occ, m.eci_vector(eci), kT, move, recycle=1)
+    e0 = float(st.energy[0])
+    e_ref = float(st.acc[0]["e_ref"])
+    bf = m.bf[0]
+    s_cur = float(np.mean(bf[occ]))
+    n = 1500
+    tr = orc.run(st, seed=3, chain_id=1, t_begin=0, n_trials=n, trace=True)
+
+    def recycled(obs, energies):  # util.waste_recycled_average
+        w = np.exp(-(energies - energies.min()) / kT)
+        return float(obs.dot(w) / w.sum())
+
+    e_cur = e0
+    cur = occ.copy()
+    sums = np.zeros(5)
+    for t in range(n):
+        energies = np.array([e_cur, e_cur + tr.de[t]])
+        w = np.exp(-(energies - energies.min()) / kT)
+        assert bool(tr.acc[t]) == bool(tr.u[t] > (w / w.sum())[0])
+        a, b = int(tr.site[2 * t]), int(tr.site[2 * t + 1])
+        s_new = s_cur
+        if tr.acc[t]:
+            if move == 0:
+                s_new += (bf[b] - bf[cur[a]]) / m.n_sites
+                cur[a] = b
+            else:
+                cur[a], cur[b] = cur[b], cur[a]
+        sl = np.array([s_cur, s_new])
+        rel = energies - e_ref
+        sums += [recycled(rel, energies), recycled(rel ** 2, energies), recycled(sl, energies),
+                 recycled(sl ** 2, energies), recycled(sl * rel, energies)]
+        if tr.acc[t]:
+            e_cur += tr.de[t]
+            s_cur = s_new
+    o = st.acc[0]
+    got = np.array([o["sum_e"], o["sum_e2"], o["sum_s"][0], o["sum_s2"][0], o["sum_se"][0]])
+    assert np.allclose(got, sums, rtol=1e-9, atol=1e-9)
+    assert np.array_equal(st.occ, cur)

@@ -500,3 +500,20 @@ def test_accept_first_trial_move_after_reset(torch_cuda):
         mc.reset()
     mc2 = Montecarlo(atoms, 1.0, seed=2)
     assert sum(mc2._mc_step()[1] for _ in range(5)) <= 5
+
+
+@pytest.mark.parametrize("sgc", [False, True])
+def test_drivers_with_waste_recycling(sgc, torch_cuda):
+    """recycle_waste=True (montecarlo.py:50-68, 937-948): the runs complete and their averages are finite."""
+    from cemc_gb300.mcmc import Montecarlo, SGCMonteCarlo
+    atoms, calc, s, eci = _calc()
+    if sgc:
+        mc = SGCMonteCarlo(atoms, 900.0, seed=4, recycle_waste=True)
+        mc.runMC(steps=3000, chem_potential={"c1_0": 0.01}, equil=False)
+        q = mc.get_thermodynamic()
+        assert np.isfinite(q["singlet_c1_0"]) and -1.0 <= q["singlet_c1_0"] <= 1.0
+    else:
+        mc = Montecarlo(atoms, 900.0, seed=4, recycle_waste=True)
+        mc.runMC(steps=3000, equil=False)
+        q = mc.get_thermodynamic()
+    assert np.isfinite(q["energy"]) and q["heat_capacity" if not sgc else "sgc_heat_capacity"] >= 0.0

@@ -531,3 +531,49 @@ def test_gpu_accept_first_matches_oracle(move, kernel, E, oracle_mod):
         assert acc[c, 0] == 1 and np.array_equal(acc[c], tr.acc)
         assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
         assert _cf_close(cb.cf.cpu().numpy()[c], st.cf)
+
+
+@pytest.mark.parametrize("move", [0, 1])
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gpu_waste_recycling_matches_oracle(prec, move, E, oracle_mod):
+    """Waste recycling (generic form, one CTA): decisions u > 1 / (1 + exp(-dE / kT)) and the weighted
+    running sums equal the oracle's (FP64 bit-exact decisions, sums to 1e-9; FP32 decisions outside the
+    near-threshold band, sums to 1e-5)."""
+    g = load_golden("ternary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    orc = oracle_mod.Oracle(m)
+    rng = np.random.default_rng(12)
+    occ = rng.integers(0, m.n_sym, (2, m.n_sites)).astype(np.int8)
+    keys = [3, 8]
+    kT = KB * np.array([600.0, 1100.0])
+    cb = E.ChainBatch(geo, occ, g["eci"], kT, move, seed=17, chain_keys=keys)
+    n = 2500
+    _, acc, de = cb.run(n, precision=prec, warps=12, trace=True, recycle_waste=True)
+    _sync()
+    cb.check_status()
+    assert cb.last_kernel == E.KERNEL_GENERIC
+    acc, de = acc.cpu().numpy(), de.cpu().numpy()
+    h = cb.accum_host()
+    for c in range(2):
+        st = orc.new_chain_state(occ[c], g["eci"], kT[c], move, recycle=1)
+        tr = orc.run(st, seed=17, chain_id=keys[c], t_begin=0, n_trials=n, trace=True)
+        if prec == 1:
+            x = tr.de / kT[c]
+            p0 = 1.0 / (1.0 + np.exp(-x))
+            near = np.abs(tr.u - p0) < 1e-5 * np.maximum(p0 * (1 - p0), 1e-300) / kT[c] + 1e-12
+            assert not np.any((acc[c] != tr.acc) & ~near)
+            if np.any(acc[c] != tr.acc):
+                continue
+        assert np.array_equal(acc[c], tr.acc)
+        assert np.array_equal(cb.occ.cpu().numpy()[c], st.occ)
+        o = st.acc[0]
+        nn = o["n_samples"]
+        tol = 1e-9 if prec == 0 else 1e-5
+        assert h[c, E.A_NSAMP] == nn and h[c, E.A_NACC] == o["n_accept"]
+        assert abs(h[c, E.A_SUM_E] - o["sum_e"]) / nn < tol * max(1.0, abs(o["sum_e"] / nn))
+        assert abs(h[c, E.A_SUM_E2] - o["sum_e2"]) / nn < tol * max(1.0, abs(o["sum_e2"] / nn))
+        for b in range(m.n_bf):
+            assert abs(h[c, E.A_SUM_S + b] - o["sum_s"][b]) / nn < tol
+            assert abs(h[c, E.A_SUM_S2 + b] - o["sum_s2"][b]) / nn < tol
+            assert abs(h[c, E.A_SUM_SE + b] - o["sum_se"][b]) / nn < tol * max(1.0, abs(o["sum_se"][b] / nn))
