@@ -1,10 +1,10 @@
 """Move constraints of the Monte Carlo drivers (cemc/mcmc/mc_constraints.py), checked on the device.
 
 The reference asks every constraint object whether a proposed move is legal
-and redraws the move until all agree (montecarlo.py:976-988).  Every
-constraint class it ships except ``PairConstraint`` decides from each change
-``(site, old symbol, new symbol)`` alone, so the device holds them as two masks
-per chain and runs the same redraw loop inside the fused kernel:
+and redraws the move until all agree (montecarlo.py:976-988).  The constraint
+classes it ships decide from each change ``(site, old symbol, new symbol)``
+alone (``PairConstraint``, as shipped, accepts every move), so the device holds
+them as two masks per chain and runs the same redraw loop inside the fused kernel:
 
 * ``frozen``: species whose sites may not change.  ``FixedElement`` compares
   the change's old symbol with its element (mc_constraints.py:95-107; the other
@@ -128,16 +128,36 @@ class FixEdgeLayers(MCConstraint):
 
 
 class PairConstraint(MCConstraint):
-    """Two elements may not share a pair cluster (mc_constraints.py:24-80).
+    """"Two elements may not share a pair cluster" (mc_constraints.py:24-80), as the reference ships it.
 
-    Its verdict depends on the neighbourhood of a change, not on the change alone, so it has no
-    device form here; ``device_masks`` rejects it.
+    The reference validates its arguments, then overwrites ``cluster_name`` with the element list
+    and hands ``str(elements)`` (e.g. "['Al', 'Mg']") to the C++ check as the cluster name
+    (mc_constraints.py:55-63); ``CEUpdater::get_clusters`` finds no cluster of that name
+    (ce_updater.cpp:879-889), so ``PairConstraint::elems_in_pair`` scans nothing and returns false
+    (pair_constraint.cpp:14-44) and every move is legal.  This class keeps the argument checks and
+    that verdict; on the device it adds no mask.
     """
 
     def __init__(self, calc=None, cluster_name=None, elements=None):
         super().__init__()
         self.name = "PairConstraint"
-        self.calc, self.cluster_name, self.elements = calc, cluster_name, elements
+        if calc is None:
+            raise ValueError("No calculator object given!")
+        if cluster_name is None:
+            raise ValueError("No cluster name given!")
+        if elements is None:
+            raise ValueError("No element list given!")
+        size = int(cluster_name[1])
+        if size != 2:
+            raise ValueError("Only pair clusters given.Given cluster has {} elements".format(size))
+        if len(elements) != 2:
+            raise ValueError("The elements list has to consist of exactly two elements")
+        self.calc = calc
+        self.cluster_name = elements  # as the reference does (mc_constraints.py:59)
+        self.elements = elements
+
+    def __call__(self, system_changes) -> bool:
+        return True
 
 
 def device_masks(constraint, symbols: Sequence[str], n_sites: int) -> Tuple[Optional[np.ndarray], int]:
@@ -162,6 +182,8 @@ def device_masks(constraint, symbols: Sequence[str], n_sites: int) -> Tuple[Opti
                 if e in sym_id:
                     allow[i] |= np.uint8(1 << sym_id[e])
         return allow, 0
+    if kind == "PairConstraint":
+        return None, 0  # accepts every move as shipped (see PairConstraint)
     if kind == "FixEdgeLayers" and hasattr(constraint, "_is_between_any") and hasattr(constraint, "pos"):
         allow = np.full(n_sites, 0xFF, dtype=np.uint8)
         pos = np.asarray(constraint.pos)
@@ -170,8 +192,8 @@ def device_masks(constraint, symbols: Sequence[str], n_sites: int) -> Tuple[Opti
                 allow[i] = 0
         return allow, 0
     raise NotImplementedError(
-        "constraint %s has no device form: the GPU drivers run FixedElement, ConstrainElementByTag and "
-        "FixEdgeLayers" % kind)
+        "constraint %s has no device form: the GPU drivers run FixedElement, ConstrainElementByTag, "
+        "FixEdgeLayers and PairConstraint" % kind)
 
 
 def combined_masks(constraints, symbols: Sequence[str], n_sites: int) -> Tuple[Optional[np.ndarray], int]:

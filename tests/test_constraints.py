@@ -67,8 +67,18 @@ def test_device_masks_match_reference_verdicts():
                 if (frozen >> old) & 1 or (allow is not None and not (int(allow[site]) >> new) & 1):
                     legal = False
             assert legal == bool(g["verdict"][k, q]), (k, g["constraint_names"][q])
+    # PairConstraint as the reference ships it accepts every move (see its docstring)
+    pc = PairConstraint(calc=object(), cluster_name="c2_d0000_0", elements=["Al", "Mg"])
+    assert pc([(0, "Al", "Mg")]) and device_masks(pc, syms, n) == (None, 0)
+    with pytest.raises(ValueError):
+        PairConstraint(calc=object(), cluster_name="c3_d0000_0", elements=["Al", "Mg"])
+
+    class Custom:
+        def __call__(self, changes):
+            return True
+
     with pytest.raises(NotImplementedError):
-        device_masks(PairConstraint(), syms, n)
+        device_masks(Custom(), syms, n)
 
 
 def _redraw_flip(rng_mod, seed, key, t, occ, movable, n_sym, allow, frozen, max_att):
