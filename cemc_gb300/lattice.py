@@ -467,7 +467,7 @@ class BackgroundSettings:
     themselves.
     """
 
-    def __init__(self, base: Settings, background_symbol: str = "O"):
+    def __init__(self, base, background_symbol: str = "O"):
         n = base.n_sites
         self.base = base
         self.cell = base.cell
@@ -478,7 +478,7 @@ class BackgroundSettings:
         self.cluster_info = base.cluster_info
         self.background_symbol = background_symbol
         self.n_sites = 2 * n
-        self.index_by_trans_symm = [list(range(n))]
+        self.index_by_trans_symm = [list(grp) for grp in base.index_by_trans_symm]  # the active sites' groups
         self.background_indices = list(range(n, 2 * n))
         self.column_sites = base.column_sites
         bg = np.arange(n, 2 * n, dtype=np.int32)
@@ -496,7 +496,7 @@ class BackgroundSettings:
         return list(active_symbols) + [self.background_symbol] * (self.n_sites // 2)
 
 
-def with_background(settings: Settings, background_symbol: str = "O") -> BackgroundSettings:
+def with_background(settings, background_symbol: str = "O") -> BackgroundSettings:
     return BackgroundSettings(settings, background_symbol)
 
 

@@ -67,6 +67,8 @@ CASES = [
     # HCP (space group P6_3/mmc): two translation groups related by a screw, 4 x 4 x 3 hexagonal cells
     ("hcp_swap", 4, 3, 2, 1, ["Mg", "Zn"], 1, 800.0, 3000, 25, None, "hcp:3"),
     ("hcp_ternary_flip", 4, 3, 2, 0, ["Al", "Mg", "Zn"], 0, 800.0, 1500, 26, None, "hcp:3"),
+    # four translation groups on the active sublattice plus an inert one
+    ("l12_background_swap", 4, 4, 2, 1, ["Li", "V"], 1, 800.0, 3000, 27, "O", "l12"),
 ]
 
 
