@@ -208,3 +208,31 @@ def test_hcp_space_group_shells_and_groups():
     for i in range(m.n_sites):
         for j in rows[i]:
             assert i in rows[j]
+
+
+@pytest.mark.parametrize("case", __import__("conftest").golden_cases())
+def test_gpu_packing_invariants(case):
+    """Per-group packing the kernels rely on, for every golden model: each group's terms are one
+    ECI-sorted range, name only its own columns, and the packed row of a site lists its group's
+    columns of the reference-shaped table; the row relation is symmetric."""
+    from conftest import golden_model, load_golden
+    g = load_golden(case)
+    s, m, eci = golden_model(g)
+    gt = m.group_terms
+    assert gt[0] == 0 and gt[-1] == m.n_terms and np.all(np.diff(gt) >= 0) and len(gt) == m.n_groups + 1
+    for q in range(m.n_groups):
+        lo, hi = int(gt[q]), int(gt[q + 1])
+        assert np.all(np.diff(m.term_eci[lo:hi]) >= 0)
+        ncol = len(m.group_cols[q])
+        for t in range(lo, hi):
+            for j in range(int(m.term_size[t]) - 1):
+                assert int(m.term_nb[t, j]) // m.n_bf < ncol
+        sites = np.nonzero(m.site_group == q)[0]
+        assert np.array_equal(m.gpu_table[np.ix_(sites, np.arange(ncol))],
+                              m.table[np.ix_(sites, np.array(m.group_cols[q]))])
+        assert np.all(m.gpu_table[sites, ncol:] == sites[:, None])
+    rows = [set(r.tolist()) for r in m.gpu_table]
+    for i in m.movable.tolist():
+        for j in rows[i]:
+            assert i in rows[j]
+    assert np.allclose(m.group_scale, m.group_count[0] / np.maximum(m.group_count, 1))
