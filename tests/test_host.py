@@ -149,3 +149,69 @@ def test_self_interaction_detection():
     assert _has_self_interaction(info)
     info = [{"c3": {"ref_indx": 0, "indices": [[1, 1]]}}]
     assert _has_self_interaction(info)
+
+
+def test_translation_group_descriptors_are_validated_on_the_host():
+    """cemc_geometry_create checks the group fields before any device call: term ranges that do not
+    cover the terms or descend, a movable site without a group, a non-positive scale, too many groups
+    and terms out of ECI order inside a group are refused with a message."""
+    from cemc_gb300 import _lib
+    from cemc_gb300.lattice import l12_settings, seeded_ecis
+    from cemc_gb300.tables import CEModel
+    try:
+        L = _lib.load()
+    except OSError as exc:  # pragma: no cover
+        pytest.skip("CUDA runtime not loadable here: %s" % exc)
+    s = l12_settings(4, 3, 2, 0, ["Al", "Mg"])
+    m = CEModel(s, list(seeded_ecis(s.cset, 0)))
+
+    def arrays():
+        return {
+            "table": np.array(m.gpu_table, dtype=np.int32, copy=True), "bf": np.array(m.bf, copy=True),
+            "kind": np.array(m.eci_kind, dtype=np.int32, copy=True),
+            "dec": np.array(m.eci_dec, dtype=np.int32, copy=True),
+            "w": np.array(m.eci_weight, copy=True), "fw": np.array(m.eci_full_weight, copy=True),
+            "te": np.array(m.term_eci, dtype=np.int32, copy=True),
+            "tr": np.array(m.term_ref, dtype=np.int32, copy=True),
+            "ts": np.array(m.term_size, dtype=np.int32, copy=True),
+            "tn": np.array(m.term_nb, dtype=np.int32, copy=True),
+            "mov": np.array(m.movable, dtype=np.int32, copy=True),
+            "sg": np.array(m.site_group, dtype=np.int32, copy=True),
+            "gt": np.array(m.group_terms, dtype=np.int32, copy=True),
+            "gs": np.array(m.group_scale, dtype=np.float64, copy=True)}
+
+    def create(h, n_groups=m.n_groups, site_group=True):
+        d = _lib.GeometryDesc(m.n_sites, m.gpu_n_cols, m.n_sym, m.n_bf, m.n_eci, m.n_terms,
+                              *[h[k].ctypes.data for k in ("table", "bf", "kind", "dec", "w", "fw", "te", "tr",
+                                                           "ts", "tn")],
+                              h["mov"].ctypes.data, len(m.movable), n_groups,
+                              h["sg"].ctypes.data if site_group else None, h["gt"].ctypes.data, h["gs"].ctypes.data)
+        handle = ctypes.c_void_p()
+        rc = L.cemc_geometry_create(ctypes.byref(d), ctypes.byref(handle))
+        buf = ctypes.create_string_buffer(256)
+        L.cemc_last_error(buf, 256)
+        if rc == _lib.OK:
+            L.cemc_geometry_destroy(handle)
+        return rc, buf.value.decode()
+
+    rc, _ = create(arrays())  # the valid descriptor passes the host checks (no GPU here: the allocation fails)
+    assert rc in (_lib.OK, _lib.ERR_CUDA)
+    h = arrays()
+    h["gt"][-1] -= 1
+    assert create(h) == (_lib.ERR_ARG, "group term ranges must cover the terms")
+    h = arrays()
+    h["gt"][1], h["gt"][2] = h["gt"][2], h["gt"][1]
+    assert create(h)[0] == _lib.ERR_ARG
+    h = arrays()
+    h["sg"][5] = m.n_groups
+    assert create(h) == (_lib.ERR_ARG, "site 5 has no translation group")
+    h = arrays()
+    h["gs"][2] = 0.0
+    assert create(h) == (_lib.ERR_ARG, "bad group scale")
+    assert create(arrays(), site_group=False) == (_lib.ERR_ARG, "null group table")
+    assert create(arrays(), n_groups=9)[0] == _lib.ERR_LIMIT
+    h = arrays()
+    lo = int(h["gt"][1])
+    h["te"][lo], h["te"][lo + 1] = h["te"][lo + 1] + 1, h["te"][lo]
+    if h["te"][lo] != h["te"][lo + 1]:
+        assert create(h)[0] == _lib.ERR_ARG
