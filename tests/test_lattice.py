@@ -236,3 +236,17 @@ def test_gpu_packing_invariants(case):
         for j in rows[i]:
             assert i in rows[j]
     assert np.allclose(m.group_scale, m.group_count[0] / np.maximum(m.group_count, 1))
+
+
+def test_generator_argument_checks():
+    """Group assignments must number the groups 0..n-1; cells too small for the cluster recipe alias
+    members onto one site and are refused."""
+    from cemc_gb300.lattice import hcp_settings, l12_settings
+    with pytest.raises(ValueError):
+        l12_settings(4, 3, 2, 0, ["Al", "Mg"], group_of_basis=(0, 2, 2, 2))
+    with pytest.raises(ValueError):
+        l12_settings(4, 3, 2, 0, ["Al", "Mg"], group_of_basis=(0, 1, 1))
+    with pytest.raises(ValueError):
+        hcp_settings(1, 1, 3, 2, 0, ["Mg", "Zn"])
+    s = l12_settings(4, 3, 2, 0, ["Al", "Mg"], group_of_basis=(0, 0, 1, 1))
+    assert [len(g) for g in s.index_by_trans_symm] == [128, 128]
