@@ -30,6 +30,7 @@ KERNEL_GENERIC = 1
 KERNEL_SPIN = 2
 KERNEL_SPIN_HALFWARP = 3
 KERNEL_TABLE = 4
+KERNEL_FIELD = 5
 MAX_BF = 4
 MAX_GROUPS = 8
 

@@ -10,8 +10,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcemc_gb300.so")
-UNITS = ["cemc_mc.cu", "cemc_cf.cu", "cemc_abi.cu"]
-HEADERS = ["cemc_device.cuh", "cemc_launch.h", "cemc_kernels.h", "cemc_spin.h", "philox.h"]
+UNITS = ["cemc_mc.cu", "cemc_field.cu", "cemc_cf.cu", "cemc_abi.cu"]
+HEADERS = ["cemc_device.cuh", "cemc_launch.h", "cemc_kernels.h", "cemc_spin.h", "cemc_field.h", "philox.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

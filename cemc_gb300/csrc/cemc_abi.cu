@@ -18,6 +18,7 @@
 #include <string>
 #include <vector>
 
+#include "cemc_field.h"
 #include "cemc_kernels.h"
 #include "cemc_spin.h"
 
@@ -47,6 +48,8 @@ struct cemc_geometry {
   cemc::DevGeo g;
   cemc::SpinDev spin{};  // tables of the binary spin-basis kernel (spin_ok)
   bool spin_ok = false;
+  cemc::FieldDev field{};  // tables of the local-field kernel (field_ok)
+  bool field_ok = false;
   void *dev = nullptr;  // one device allocation holding every table
   int max_smem = 0;     // opt-in shared memory per block of the current device
   int n_sms = 0;        // multiprocessors of the current device
@@ -370,6 +373,123 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       }
     }
   }
+  // Local-field form (single-site flips in the spin basis, cemc_field.h): one
+  // count field per cluster ECI, packed into at most two words per site, and
+  // the update list of a changed site j, derived from site 0's neighbourhood
+  // and verified to hold at every site (a periodic supercell of one
+  // translation group); rows must list distinct sites other than the site.
+  bool field_ok = spin_ok && n_movable == N && N <= cemc::kFieldMaxSites &&
+                  (int)spin_eci.size() <= cemc::kFieldMaxCl;
+  int field_pw = 1;
+  std::vector<int32_t> f_slot_eci, f_ustart(C + 1, 0);
+  std::vector<uint32_t> f_meta, f_cnt, f_pairinc, f_upd;
+  if (field_ok) {
+    const int ncl = (int)spin_eci.size();
+    std::vector<int> fword(ncl, 0), fshift(ncl, 0);
+    int word = 0, used = 0;
+    for (int q = 0; q < ncl && field_ok; ++q) {
+      const int Kq = spin_eci[q].n_pairs + spin_eci[q].n_multi;
+      int bits = 1;
+      while ((1 << bits) <= Kq) ++bits;
+      if (Kq > 255) field_ok = false;
+      if (used + bits > 32) {
+        ++word;
+        used = 0;
+      }
+      if (word > 1) field_ok = false;
+      fword[q] = word;
+      fshift[q] = used;
+      used += bits;
+      f_slot_eci.push_back(spin_eci[q].eci);
+      f_meta.push_back((uint32_t)Kq | ((uint32_t)fshift[q] << 8) | ((uint32_t)word << 13) | ((uint32_t)bits << 16));
+    }
+    field_pw = word + 1;
+    auto add_inc = [&](int q, uint32_t *w) { w[fword[q]] += 1u << fshift[q]; };
+    // (site, column) keys of every row, sorted by site: the column of a site in a row
+    std::vector<uint64_t> keys(field_ok ? (size_t)N * C : 0);
+    for (int i = 0; i < N && field_ok; ++i) {
+      uint64_t *k = keys.data() + (size_t)i * C;
+      for (int c = 0; c < C; ++c) {
+        const int s = d->table[(size_t)i * C + c];
+        if (s == i) field_ok = false;
+        k[c] = ((uint64_t)(uint32_t)s << 8) | (uint64_t)c;
+      }
+      std::sort(k, k + C);
+      for (int c = 1; c < C; ++c)
+        if ((k[c] >> 8) == (k[c - 1] >> 8)) field_ok = false;
+    }
+    auto col_of = [&](int i, int x) -> int {
+      const uint64_t *b = keys.data() + (size_t)i * C, *e = b + C;
+      const uint64_t *p = std::lower_bound(b, e, (uint64_t)(uint32_t)x << 8);
+      return (p != e && (*p >> 8) == (uint64_t)(uint32_t)x) ? (int)(*p & 255u) : -1;
+    };
+    std::vector<int> inv(C, -1);  // row_{row_j[c]}[inv[c]] = j
+    for (int c = 0; c < C && field_ok; ++c) {
+      inv[c] = col_of(d->table[c], 0);
+      if (inv[c] < 0) field_ok = false;
+    }
+    std::vector<std::array<int, 3>> cmap;  // (c, c2, c3): row_j[c3] = row_{row_j[c]}[c2]
+    if (field_ok) {
+      for (int q = 0; q < ncl; ++q) {  // count entries: pair shells, then multi-site terms
+        uint32_t w[2] = {0, 0};
+        add_inc(q, w);
+        f_cnt.insert(f_cnt.end(), {spin_eci[q].pair_lo, spin_eci[q].pair_hi, w[0], w[1]});
+      }
+      for (int t = 0; t < n_masks; ++t) {
+        uint32_t w[2] = {0, 0};
+        add_inc(spin_mask_cl[t], w);
+        f_cnt.insert(f_cnt.end(), {spin_masks[2 * t], spin_masks[2 * t + 1], w[0], w[1]});
+      }
+      for (int c = 0; c < C && field_ok; ++c) {
+        f_ustart[c] = (int32_t)(f_upd.size() / 4);
+        const int i = d->table[c];  // the target row_0[c]
+        const int cp = inv[c];      // site 0 seen from the target
+        const uint64_t bit = (uint64_t)1 << cp;
+        uint32_t pinc[2] = {0, 0};
+        for (int q = 0; q < ncl; ++q)
+          if ((((uint64_t)spin_eci[q].pair_hi << 32) | spin_eci[q].pair_lo) & bit) add_inc(q, pinc);
+        f_pairinc.insert(f_pairinc.end(), {pinc[0], pinc[1]});
+        for (int t = 0; t < n_masks && field_ok; ++t) {
+          const uint64_t m = ((uint64_t)spin_masks[2 * t + 1] << 32) | spin_masks[2 * t];
+          if (!(m & bit)) continue;
+          uint64_t others = m & ~bit, mj = 0;
+          while (others) {
+            const int c2 = __builtin_ctzll(others);
+            others &= others - 1;
+            const int c3 = col_of(0, d->table[(size_t)i * C + c2]);
+            if (c3 < 0) {
+              field_ok = false;
+              break;
+            }
+            mj |= (uint64_t)1 << c3;
+            cmap.push_back({c, c2, c3});
+          }
+          uint32_t w[2] = {0, 0};
+          add_inc(spin_mask_cl[t], w);
+          f_upd.insert(f_upd.end(), {(uint32_t)mj, (uint32_t)(mj >> 32), w[0], w[1]});
+        }
+      }
+      f_ustart[C] = (int32_t)(f_upd.size() / 4);
+      std::sort(cmap.begin(), cmap.end());
+      cmap.erase(std::unique(cmap.begin(), cmap.end()), cmap.end());
+    }
+    for (int j = 1; j < N && field_ok; ++j) {
+      const int32_t *rj = d->table + (size_t)j * C;
+      for (int c = 0; c < C; ++c)
+        if (col_of(rj[c], j) != inv[c]) field_ok = false;
+      for (const auto &m : cmap)
+        if (col_of(j, d->table[(size_t)rj[m[0]] * C + m[1]]) != m[2]) field_ok = false;
+    }
+  }
+  if (!field_ok) {
+    f_slot_eci.assign(1, 0);
+    f_meta.assign(1, 0u);
+    f_cnt.assign(4, 0u);
+    f_pairinc.assign(2 * (size_t)C, 0u);
+    f_ustart.assign(C + 1, 0);
+    f_upd.assign(4, 0u);
+  }
+  if (f_upd.empty()) f_upd.assign(4, 0u);
   if (half_shift.empty()) half_shift.assign(1, 0);
   if (spin_eci.empty()) spin_eci.push_back(cemc::SpinEci{});
   if (spin_masks.empty()) spin_masks.assign(2, 0u);
@@ -405,6 +525,12 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {sgroup.data(), sgroup.size(), 0},
       {geo_start.data(), geo_start.size() * 4, 0},
       {gscale.data(), gscale.size() * 8, 0},
+      {f_slot_eci.data(), f_slot_eci.size() * 4, 0},
+      {f_meta.data(), f_meta.size() * 4, 0},
+      {f_cnt.data(), f_cnt.size() * 4, 0},
+      {f_pairinc.data(), f_pairinc.size() * 4, 0},
+      {f_ustart.data(), f_ustart.size() * 4, 0},
+      {f_upd.data(), f_upd.size() * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -484,6 +610,19 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   geo->spin.half_shift = reinterpret_cast<const uint8_t *>(base + parts[18].off);
   geo->spin.half_lane_term = reinterpret_cast<const int32_t *>(base + parts[19].off);
   geo->spin.half_lane_first = reinterpret_cast<const int32_t *>(base + parts[20].off);
+  geo->field_ok = field_ok;
+  geo->field.n_cl = field_ok ? (int)f_slot_eci.size() : 0;
+  geo->field.pw = field_pw;
+  geo->field.n_cnt = field_ok ? (int)(f_cnt.size() / 4) : 0;
+  geo->field.n_upd = field_ok ? (int)f_ustart[C] : 0;
+  geo->field.minus_id = minus_id;
+  geo->field.singlet_eci = singlet_eci;
+  geo->field.slot_eci = reinterpret_cast<const int32_t *>(base + parts[29].off);
+  geo->field.slot_meta = reinterpret_cast<const uint32_t *>(base + parts[30].off);
+  geo->field.cnt = reinterpret_cast<const uint4 *>(base + parts[31].off);
+  geo->field.pairinc = reinterpret_cast<const uint2 *>(base + parts[32].off);
+  geo->field.ustart = reinterpret_cast<const int32_t *>(base + parts[33].off);
+  geo->field.upd = reinterpret_cast<const uint4 *>(base + parts[34].off);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&geo->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -522,7 +661,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
   r->kernel_used = CEMC_KERNEL_AUTO;  // nothing launched yet
   if (r->n_trials == 0) return CEMC_OK;
-  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_TABLE)
+  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_FIELD)
     return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
   if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
   // waste recycling runs its own build of the generic form, one CTA per chain
@@ -545,6 +684,65 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
     return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs unconstrained single-site flips with at most 16 "
                               "cluster ECIs");
+  // Local-field form: unconstrained single-site flips of a geometry with field tables, one CTA
+  // per chain, when asked for (its state fits in shared memory, with the conflict table in the
+  // caller's stamp buffer when it does not fit beside the counts).
+  const bool field_possible = geo->field_ok && r->move == CEMC_MOVE_FLIP && !constrained && r->cluster != 2;
+  if (r->kernel == CEMC_KERNEL_FIELD && !field_possible)
+    return fail(CEMC_ERR_ARG, "the local-field kernel runs unconstrained single-site flips of a periodic binary "
+                              "+1/-1 geometry of one translation group without background sites, one CTA per chain");
+  if (field_possible && r->kernel == CEMC_KERNEL_FIELD) {
+    const cemc::FieldDev &fd = geo->field;
+    cemc::RunArgs fa{};
+    fa.n_chains = r->n_chains;
+    fa.warps = r->warps > 0 ? std::min(r->warps, cemc::kFieldMaxWarps) : 16;
+    fa.cl = 1;
+    fa.tpw = 1;
+    fa.ring_bits = cemc::field_ring_bits(cemc::field_round(fa.warps));
+    fa.occ_smem = 1;
+    int bits = 5;
+    while ((1 << bits) < g.n_sites) ++bits;
+    fa.stamp_bits = bits;
+    const int rs = r->precision == CEMC_PREC_F32 ? 4 : 8;
+    size_t smem = cemc::field_layout(g, fd.n_cl, fd.pw, fd.n_cnt, fd.n_upd, rs, fa.ring_bits, false).total;
+    if (smem > (size_t)geo->max_smem && r->stamps && r->stamp_words >= cemc_stamp_words(geo, r->n_chains)) {
+      fa.gstamp = r->stamps;
+      smem = cemc::field_layout(g, fd.n_cl, fd.pw, fd.n_cnt, fd.n_upd, rs, fa.ring_bits, true).total;
+    }
+    if (smem <= (size_t)geo->max_smem) {
+      fa.seed = r->seed;
+      fa.occ = r->occ;
+      fa.cf = r->cf;
+      fa.energy = r->energy;
+      fa.eci = r->eci;
+      fa.kT = r->kT;
+      fa.trial = r->trial;
+      fa.accum = r->accum;
+      fa.trace_site = r->trace_site;
+      fa.trace_acc = r->trace_acc;
+      fa.trace_de = r->trace_de;
+      fa.status = r->status;
+      fa.chain_key = r->chain_key;
+      fa.accum_slot = r->accum_slot;
+      fa.chain_trials = r->chain_trials;
+      const uint64_t max_chunk = (uint64_t)1 << 25;  // round numbers fit the 26 upper bits of a stamp
+      if (r->n_trials > max_chunk && r->trace_acc)
+        return fail(CEMC_ERR_LIMIT, "traced runs are limited to %llu trials per call", (unsigned long long)max_chunk);
+      for (uint64_t done = 0; done < r->n_trials;) {
+        const uint64_t n = std::min(max_chunk, r->n_trials - done);
+        fa.n_trials = n;
+        fa.chunk_offset = done;
+        cudaError_t e = cemc::launch_field(g, fa, fd, r->precision, smem, static_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return cuda_fail(e, "local-field Monte Carlo kernel launch");
+        done += n;
+      }
+      r->kernel_used = CEMC_KERNEL_FIELD;
+      return CEMC_OK;
+    }
+    if (r->kernel == CEMC_KERNEL_FIELD)
+      return fail(CEMC_ERR_LIMIT, "the local-field kernel needs %zu bytes of shared memory (limit %d); pass a stamp "
+                                  "buffer or use another kernel", smem, geo->max_smem);
+  }
   // two trials per warp: asked for, or chosen when eligible and no CTA pair was asked for
   // (a CTA pair takes the half-warp form only when that form is asked for explicitly)
   const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&

@@ -201,6 +201,9 @@ typedef struct {
 #define CEMC_KERNEL_SPIN 2
 #define CEMC_KERNEL_SPIN_HALFWARP 3  /* spin basis, flips only, two trials per warp (one per 16 lanes) */
 #define CEMC_KERNEL_TABLE 4  /* one table lookup per cluster geometry; CFs and energies by a final recompute */
+#define CEMC_KERNEL_FIELD 5  /* local field: spin basis, unconstrained flips of a periodic one-group supercell;
+                                every site keeps its per-ECI odd-term counts in shared memory, a trial reads
+                                them (one lane per trial) and an accepted flip updates its neighbours' counts */
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
  * energy change, accept test and in-place commit of occupation, correlation
