@@ -167,17 +167,14 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the MC kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "mc_kernel_sgc_64x16384.md")
-    try:
-        with open(path) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":", 1)[1].split()[0])
-    except Exception:
-        pass
-    return None
+# Figures of the headline MC kernel that only a profiler measures (one ncu capture of one
+# 10-sweep launch of this kernel on this workload, --clock-control none): DRAM bytes read +
+# written per launch (the one-time read of the occupations and the neighbour table after the
+# L2 flush; it does not grow with the sweep count) and warp instructions issued per cycle on
+# the SMs that hold a chain.  They are reported with that source, never as this run's numbers.
+NCU_MC_TRAFFIC_BYTES = 4828672.0
+NCU_MC_IPC_ACTIVE_SM = 2.23
+NCU_SOURCE = "ncu capture of one 10-sweep launch of the same kernel and workload"
 
 
 def cpu_port_rate(m, occ, ev, Ts, sample_sweeps: float, threads: int, seed: int = 7):
@@ -593,7 +590,8 @@ def run_gpu(args):
     alg_bytes = bytes_per_flip * trials_per_step
     achieved = alg_bytes / (k_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = profiled_traffic()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    busy_sms = min(sms, N_CHAINS * max(1, runner.cluster))
 
     # -- end to end through the public batched API, host buffers each step ---------------
     occ_h = torch.from_numpy(occ).pin_memory()
@@ -657,9 +655,14 @@ def run_gpu(args):
             "gpu_launches": n_launches,
             "clocks": clocks,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "mc_kernel<float, flip>", "kernel_ms": k_ms,
-                         "alg_bytes_per_trial": bytes_per_flip},
+                         "frac": achieved / peak, "traffic": NCU_MC_TRAFFIC_BYTES, "traffic_source": NCU_SOURCE,
+                         "peak_kind": peak_kind, "kernel": "mc_kernel<float, flip>", "kernel_ms": k_ms,
+                         "alg_bytes_per_trial": bytes_per_flip,
+                         "note": "HBM does not bind: after the first sweep the kernel works from shared memory "
+                                 "and L2; the issue bound below is the one that binds"},
+            "issue_bound": {"sms_holding_a_chain": busy_sms, "sms": sms, "sm_fraction": busy_sms / sms,
+                            "ipc_per_busy_sm": NCU_MC_IPC_ACTIVE_SM, "ipc_source": NCU_SOURCE,
+                            "frac_of_gpu_issue": NCU_MC_IPC_ACTIVE_SM * busy_sms / (4.0 * sms)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain_gpu": {"value": plain, "unit": UNIT,
                           "form": "one chain per launch, FP64 energy change, one sweep per launch, no graph"},

@@ -795,11 +795,13 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
     forms = {cemc::kFormRecycle};
   else if (use_spin)
     forms = {cemc::kFormSpin};
+  else if (r->kernel == CEMC_KERNEL_TABLE && r->n_chains > 65535)
+    return fail(CEMC_ERR_LIMIT, "the table kernel ends with a recompute of at most 65535 chains per call");
   else if (r->kernel == CEMC_KERNEL_TABLE)
     forms = {cemc::kFormTable};
   else if (r->kernel == CEMC_KERNEL_GENERIC)
     forms = {cemc::kFormGeneric};
-  else if (g.table_ok)
+  else if (g.table_ok && r->n_chains <= 65535)
     forms = {cemc::kFormTable, cemc::kFormGeneric};
   else
     forms = {cemc::kFormGeneric};
@@ -878,7 +880,10 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   double *rscratch = nullptr;
   if (form == cemc::kFormTable) {
     const size_t need = cemc::recompute_blocks(g) * (size_t)r->n_chains * (size_t)g.n_eci;
-    if (r->scratch && r->scratch_doubles >= need) {
+    if (r->scratch && r->scratch_doubles < need)
+      return fail(CEMC_ERR_ARG, "the table kernel's final recompute needs a scratch buffer of %zu doubles, the run "
+                                "descriptor gives %llu", need, (unsigned long long)r->scratch_doubles);
+    if (r->scratch) {
       rscratch = r->scratch;
     } else if (need <= cemc::kNoAllocScratchDoubles) {
       cudaError_t err = cudaSuccess;

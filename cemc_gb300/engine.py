@@ -321,7 +321,8 @@ class ChainBatch:
                          _ptr(self.trk_start), _ptr(self.trk_count),
                          _ptr(tr[0]) if tr else None, _ptr(tr[1]) if tr else None, _ptr(tr[2]) if tr else None,
                          _ptr(self.status), _ptr(self.chain_key), _ptr(getattr(self, "accum_slot", None)),
-                         _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch), self.scratch.numel(),
+                         _ptr(chain_trials), int(kernel), int(cluster), _ptr(self.scratch),
+                         self.scratch.numel() if self.scratch is not None else 0,
                          _ptr(self._stamps()), self._stamp_buf.numel() if self._stamp_buf is not None else 0,
                          0, _ptr(site_allow), _ptr(frozen), int(max_attempts), int(bool(accept_first)),
                          int(bool(recycle_waste)))

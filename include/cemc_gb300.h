@@ -159,8 +159,13 @@ typedef struct {
   int32_t kernel;      /* CEMC_KERNEL_*: which implementation runs the trials */
   int32_t cluster;     /* CTAs per chain: 1, 2 (a thread-block cluster pair on two SMs, twice the trials
                           per round), or 0 = 2 when every chain's pair fits on the GPU at once, else 1 */
-  double *scratch;     /* table kernel: buffer for the final recompute (cemc_recompute_scratch_doubles()
-                          doubles); NULL = the library's fixed array when it is large enough */
+  double *scratch;     /* table kernel: buffer for the final recompute, at least cemc_recompute_scratch_doubles()
+                          doubles (a smaller buffer is refused with CEMC_ERR_ARG).  NULL = the fixed array
+                          behind cemc_recompute_noalloc(), under the same rules: at most 1048576 doubles
+                          (CEMC_ERR_LIMIT beyond), the first such call on a device looks up the array's
+                          address and should come before any stream capture, and every call that uses
+                          the array shares it, so such calls (and cemc_recompute_noalloc calls) that
+                          overlap on the GPU race: order them on one stream. */
   uint64_t scratch_doubles;
   uint32_t *stamps;    /* optional device buffer for exact conflict tables of large supercells, used when
                           the shared-memory table would have to be hashed (hashing only costs speed):
@@ -240,8 +245,10 @@ int cemc_recompute(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ
  * device address (cudaGetSymbolAddress) with that device current; make that
  * first call before any stream capture.  All calls share the one array, so
  * calls that overlap on the GPU (other streams, other threads) race: order
- * them on one stream or synchronise between them.  It never calls cudaMalloc,
- * cudaFree or an allocating library routine. */
+ * them on one stream or synchronise between them.  The array's address is
+ * cached per device ordinal for the life of the process, so the library must
+ * not be used on a device again after cudaDeviceReset() there.  It never calls
+ * cudaMalloc, cudaFree or an allocating library routine. */
 int cemc_recompute_noalloc(const cemc_geometry *geo, int32_t n_chains, const int8_t *occ, const double *eci,
                            double *cf, double *energy, void *stream);
 

@@ -11,7 +11,7 @@
 # Needs cython, g++, Python and numpy headers; exits 0 with a message when the
 # reference tree is absent (as on machines that only run the product).
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${CEMC_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/cpp/src" ]; then

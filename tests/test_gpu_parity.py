@@ -585,3 +585,33 @@ def test_gpu_waste_recycling_matches_oracle(prec, move, E, oracle_mod):
             assert abs(h[c, E.A_SUM_S + b] - o["sum_s"][b]) / nn < tol
             assert abs(h[c, E.A_SUM_S2 + b] - o["sum_s2"][b]) / nn < tol
             assert abs(h[c, E.A_SUM_SE + b] - o["sum_se"][b]) / nn < tol * max(1.0, abs(o["sum_se"][b] / nn))
+
+
+def test_gpu_table_form_scratch_rules(E):
+    """cemc_run's table form ends with a full recompute: with no scratch buffer it uses the library's fixed
+    array and gives the same chains as with a caller buffer; a caller buffer that is too small is refused
+    (CEMC_ERR_ARG) before anything is launched."""
+    import torch
+    from cemc_gb300._lib import CemcError, ERR_ARG
+    g = load_golden("ternary_swap")
+    s, m, eci = golden_model(g)
+    geo = E.Geometry(m)
+    rng = np.random.default_rng(31)
+    occ = rng.integers(0, m.n_sym, (3, m.n_sites)).astype(np.int8)
+    a = E.ChainBatch(geo, occ, g["eci"], KB * 900.0, 1, seed=12)
+    b = E.ChainBatch(geo, occ, g["eci"], KB * 900.0, 1, seed=12)
+    a.run(3000, precision=E.PREC_F32, warps=8, kernel=E.KERNEL_TABLE)
+    b.scratch = None  # the fixed array
+    b.run(3000, precision=E.PREC_F32, warps=8, kernel=E.KERNEL_TABLE)
+    _sync()
+    assert a.last_kernel == b.last_kernel == E.KERNEL_TABLE
+    assert torch.equal(a.occ, b.occ)
+    assert torch.equal(a.cf, b.cf) and torch.equal(a.energy, b.energy)
+    c = E.ChainBatch(geo, occ, g["eci"], KB * 900.0, 1, seed=12)
+    occ_before = c.occ.clone()
+    c.scratch = torch.empty(1, dtype=torch.float64, device="cuda")
+    with pytest.raises(CemcError) as ei:
+        c.run(3000, precision=E.PREC_F32, warps=8, kernel=E.KERNEL_TABLE)
+    assert ei.value.code == ERR_ARG
+    _sync()
+    assert torch.equal(c.occ, occ_before)
