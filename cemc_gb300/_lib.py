@@ -102,6 +102,8 @@ def load():
         L.cemc_recompute_scratch_doubles.restype = C.c_size_t
         L.cemc_recompute_scratch_doubles.argtypes = [_P, C.c_int32]
         L.cemc_recompute.argtypes = [_P, C.c_int32, _P, _P, _P, _P, _P, _P]
+        L.cemc_geometry_device_bytes.restype = C.c_size_t
+        L.cemc_geometry_device_bytes.argtypes = [_P]
         L.cemc_stamp_words.restype = C.c_size_t
         L.cemc_stamp_words.argtypes = [_P, C.c_int32]
         L.cemc_energy.argtypes = [_P, C.c_int32, _P, _P, _P, _P]
@@ -130,8 +132,8 @@ def exported_symbols():
     """Names declared in include/cemc_gb300.h that the loaded library exports."""
     L = load()
     names = []
-    for n in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_run", "cemc_recompute_scratch_doubles",
-              "cemc_stamp_words", "cemc_recompute", "cemc_recompute_noalloc", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
+    for n in ("cemc_geometry_create", "cemc_geometry_destroy", "cemc_geometry_device_bytes", "cemc_run",
+              "cemc_recompute_scratch_doubles", "cemc_stamp_words", "cemc_recompute", "cemc_recompute_noalloc", "cemc_energy", "cemc_apply_changes", "cemc_delta_e", "cemc_pt_exchange", "cemc_last_error",
               "cemc_version"):
         if hasattr(L, n):
             names.append(n)

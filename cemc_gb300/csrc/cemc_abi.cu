@@ -51,6 +51,7 @@ struct cemc_geometry {
   cemc::FieldDev field{};  // tables of the local-field kernel (field_ok)
   bool field_ok = false;
   void *dev = nullptr;  // one device allocation holding every table
+  size_t dev_bytes = 0;  // its size
   int max_smem = 0;     // opt-in shared memory per block of the current device
   int n_sms = 0;        // multiprocessors of the current device
   // resident cluster pairs per launch configuration (warps, move, precision, spin, smem)
@@ -538,6 +539,7 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
     total = align_up(total + p.bytes, 256);
   }
   cemc_geometry *geo = new cemc_geometry();
+  geo->dev_bytes = total;
   cudaError_t e = cudaMalloc(&geo->dev, total);
   if (e != cudaSuccess) {
     delete geo;
@@ -638,6 +640,8 @@ extern "C" int cemc_geometry_destroy(cemc_geometry *geo) {
   if (e != cudaSuccess) return cuda_fail(e, "cudaFree(geometry tables)");
   return CEMC_OK;
 }
+
+extern "C" size_t cemc_geometry_device_bytes(const cemc_geometry *geo) { return geo ? geo->dev_bytes : 0; }
 
 extern "C" size_t cemc_stamp_words(const cemc_geometry *geo, int32_t n_chains) {
   if (!geo || n_chains <= 0) return 0;

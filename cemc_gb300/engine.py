@@ -116,6 +116,13 @@ class Geometry:
     def scratch_doubles(self, n_chains: int) -> int:
         return int(self.L.cemc_recompute_scratch_doubles(self.handle, n_chains))
 
+    def device_bytes(self) -> int:
+        """Device memory of the geometry's tables (``cemc_geometry_device_bytes``)."""
+        return int(self.L.cemc_geometry_device_bytes(self.handle))
+
+    def stamp_words(self, n_chains: int) -> int:
+        return int(self.L.cemc_stamp_words(self.handle, n_chains))
+
 
 def build_tracker(occ: np.ndarray, n_sym: int, background=None):
     """Per-species site lists of swap moves: sites of each species in site order.

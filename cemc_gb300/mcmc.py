@@ -87,6 +87,7 @@ class Montecarlo:
         self.max_allowed_constraint_pass_attempts = int(max_constraint_attempts)
         self._constraint_dev = None  # device masks of self.constraints, built on first use
         self.bias_potentials = []
+        self.bias_energy = 0.0
         self.current_step = 0
         self.num_accepted = 0
         self.status_every_sec = 30
@@ -149,7 +150,13 @@ class Montecarlo:
             raise TooFewElementsError("There is only one element that has more than one atom")
 
     def update_current_energy(self):
+        """Energy of the current state from the calculator plus every bias potential's value,
+        computed from scratch (montecarlo.py:276-282)."""
         self.current_energy = self._calc().get_energy()
+        self.bias_energy = 0.0
+        for bias in self.bias_potentials:
+            self.bias_energy += float(bias.calculate_from_scratch(self.atoms))
+        self.current_energy += self.bias_energy
 
     def set_symbols(self, symbs):
         self._calc().set_symbols(symbs)
@@ -249,7 +256,22 @@ class Montecarlo:
             raise RuntimeError("Could insert {} {} atoms!".format(num, symbol))
 
     def add_bias(self, potential):
-        raise NotImplementedError("bias potentials are not supported by the GPU drivers")
+        """Add a bias potential (montecarlo.py:394-401).
+
+        A bias is any object with the reference's ``BiasPotential`` interface
+        (cemc/mcmc/bias_potential.py:4-31): ``potential(system_changes)`` returns its value
+        for the state after the proposed changes, which the acceptance test adds to that
+        state's energy (montecarlo.py:925-930); ``calculate_from_scratch(atoms)`` gives its
+        value for the current state.  Arbitrary host code cannot run inside the kernel, so a
+        driver with biases evaluates its trials one at a time on the host (``_run_biased``):
+        the same counter-based proposals and uniforms as the kernel, the energy change from the
+        device calculator, the biases, then the reference's acceptance test.
+        """
+        if not callable(potential) or not hasattr(potential, "calculate_from_scratch"):
+            raise TypeError("potential has to be of type BiasPotential")
+        if self.recycle_waste:
+            raise NotImplementedError("waste recycling together with bias potentials is not supported")
+        self.bias_potentials.append(potential)
 
     def attach(self, obs, interval=1):
         """Call ``obs(system_changes)`` every ``interval`` trials (montecarlo.py:403-415).
@@ -288,6 +310,8 @@ class Montecarlo:
         ``(site, old, old)`` when it was rejected).  The trials between two such steps
         run as one launch; the observed trial runs alone, traced.
         """
+        if self.bias_potentials:
+            return self._run_biased(n, trace)
         traces = []
         done = 0
         while done < n:
@@ -347,6 +371,147 @@ class Montecarlo:
                 obs(changes)
         return [tr] if trace else []
 
+    def _run_biased(self, n: int, trace: bool = False):
+        """n trials of a driver with bias potentials, one at a time (the reference's _mc_step and
+        _accept, montecarlo.py:910-1038).
+
+        Trial t draws its proposal and uniform from the same counter-based stream as the kernel
+        (proposal k of a redrawn trial from streams 2k, 2k + 1), so a biased run continues the
+        chain an unbiased launch would continue, and the device trial counter, swap site lists
+        and running sums stay valid.  Per trial: the energy change from the device calculator
+        (``cemc_delta_e``), the atoms object updated to the proposed state and each bias called
+        with the changes, then accept when new < current or u <= exp(-(new - current) / kT)
+        (the first trial after a reset is accepted outright when asked), commit on the device
+        (``cemc_apply_changes``).  The running sums take the energy with its bias, as the
+        reference's averages do.
+        """
+        from .rng import below, trial_draw, u01_53
+        calc = self._calc()
+        up = calc.updater
+        m = calc.model
+        ch = self.chain()
+        torch.cuda.synchronize(ch.occ.device)
+        key = int(ch.chain_key[0].item())
+        t = int(ch.trial[0].item())
+        occ = up.occupation().astype(np.int64)
+        swap = self.move == E.MOVE_SWAP
+        if swap:
+            trk, loc = ch.trk[0].cpu().numpy().copy(), ch.loc[0].cpu().numpy().copy()
+            start, count = ch.trk_start[0].cpu().numpy(), ch.trk_count[0].cpu().numpy()
+            present = [s for s in range(m.n_sym) if count[s] > 0]
+        movable = np.asarray(m.movable, dtype=np.int64)
+        every_site = len(movable) == m.n_sites
+        syms = m.symbols
+        e_ref = float(ch.accum_host()[0, E.A_EREF])
+        cf = up.cf()
+        sing_idx = [int(k) for k in m.singlet_eci[:m.n_bf]]
+        sing = np.array([cf[k] for k in sing_idx], dtype=np.float64)
+        e_ce = up.energy()
+        sums = np.zeros(E.A_NSAMP - 1)  # sum_e, sum_e2, sum_s[4], sum_s2[4], sum_se[4]
+        n_acc = 0
+        kT = self._kT()
+        max_att = self.max_allowed_constraint_pass_attempts
+        tr_sites, tr_acc, tr_de = [], [], []
+
+        def proposal(k):
+            w = trial_draw(self.seed, key, t, 2 * k)
+            if swap:
+                x = trial_draw(self.seed, key, t, 2 * k + 1)
+                npres = len(present)
+                ia = below(w[0], npres)
+                ib = below(w[1], npres - 1)
+                ib += ib >= ia
+                A, B = present[ia], present[ib]
+                a = int(trk[start[A] + below(w[2], int(count[A]))])
+                b = int(trk[start[B] + below(w[3], int(count[B]))])
+                return [(a, A, B), (b, B, A)], x[0], x[1]
+            a = int(below(w[0], m.n_sites)) if every_site else int(movable[below(w[0], len(movable))])
+            old = int(occ[a])
+            kk = below(w[1], m.n_sym - 1)
+            return [(a, old, kk + (kk >= old))], w[2], w[3]
+
+        for _ in range(n):
+            self.current_step += 1
+            k = 0
+            ids, ua, ub = proposal(0)
+            while not self._no_constraint_violations([(s, syms[o], syms[v]) for s, o, v in ids]) and k < max_att:
+                k += 1
+                ids, ua, ub = proposal(k)
+            if k == max_att:
+                raise CanNotFindLegalMoveError("Did not manage to produce a trial move that does not violate any "
+                                               "of the constraints")
+            t += 1
+            changes = [(s, syms[o], syms[v]) for s, o, v in ids]
+            if swap:
+                de, dcf = up.delta_swap(ids[0][0], ids[1][0])
+            else:
+                de, dcf = up.delta_flip(ids[0][0], ids[0][2])
+            # the biases see the system with the proposed changes in place (montecarlo.py:925-930)
+            for s, _, v in changes:
+                self.atoms[s].symbol = v
+            bias_new = 0.0
+            for bias in self.bias_potentials:
+                bias_new += float(bias(changes))
+            new_energy = e_ce + de + bias_new
+            if self.is_first:
+                self.is_first = False
+                accept = True
+            elif new_energy < self.current_energy:
+                accept = True
+            else:
+                accept = u01_53(ua, ub) <= np.exp(-(new_energy - self.current_energy) / kT)
+            tr_sites.append((ids[0][0], ids[1][0] if swap else ids[0][2]))
+            tr_acc.append(int(accept))
+            tr_de.append(new_energy - self.current_energy)
+            if accept:
+                up.apply(ids, record=False)
+                e_ce += de
+                self.current_energy = new_energy
+                self.bias_energy = bias_new
+                for s, _, v in ids:
+                    occ[s] = v
+                if swap:  # the site lists as the kernel's commit leaves them
+                    (a, A, B), (b, _, _) = ids
+                    la, lb = int(loc[a]), int(loc[b])
+                    trk[start[A] + la] = b
+                    loc[b] = la
+                    trk[start[B] + lb] = a
+                    loc[a] = lb
+                sing += np.array([dcf[k] for k in sing_idx])
+                n_acc += 1
+                obs_changes = changes
+            else:
+                for s, o, _ in changes:
+                    self.atoms[s].symbol = o
+                obs_changes = [(s, o, o) for s, o, _ in changes]
+            e = self.current_energy - e_ref
+            sums[0] += e
+            sums[1] += e * e
+            for b in range(m.n_bf):
+                sums[2 + b] += sing[b]
+                sums[2 + E._lib.MAX_BF + b] += sing[b] * sing[b]
+                sums[2 + 2 * E._lib.MAX_BF + b] += sing[b] * e
+            for interval, obs in self.observers:
+                if int(interval) > 0 and self.current_step % int(interval) == 0:
+                    obs(obs_changes)
+        # hand the chain back to the device path: trial counter, site lists, running sums
+        raw = ch.accum.cpu().numpy().copy()
+        raw[0, E.A_SUM_E:E.A_NSAMP] += sums
+        counters = raw[0, E.A_NSAMP:E.A_NACC + 1].view(np.uint64)
+        counters += np.array([n, n_acc], dtype=np.uint64)
+        ch.accum.copy_(torch.as_tensor(raw))
+        ch.trial.fill_(t)
+        if swap:
+            ch.trk[0].copy_(torch.as_tensor(trk))
+            ch.loc[0].copy_(torch.as_tensor(loc))
+        up.clear()
+        self.num_accepted = int(ch.accum_host()[0, E.A_NACC])
+        if not trace:
+            return []
+        sites = torch.tensor(tr_sites, dtype=torch.int32).view(1, n, 2)
+        return [(sites, torch.tensor(tr_acc, dtype=torch.int8).view(1, n),
+                 torch.tensor(tr_de, dtype=torch.float64).view(1, n))]
+
     def _warps(self):
         if self.warps:
             return self.warps
@@ -380,7 +545,10 @@ class Montecarlo:
 
     def _mc_step(self, verbose=False):
         """One trial (the reference's _mc_step, observers included); returns (energy, accepted)."""
-        (_, acc, _), = self._observed_trial(trace=True)
+        if self.bias_potentials:
+            (_, acc, _), = self._run_biased(1, trace=True)
+        else:
+            (_, acc, _), = self._observed_trial(trace=True)
         return self.current_energy, bool(acc.cpu().numpy()[0, 0])
 
     def _probe_energy_bias(self, num_steps=1000):

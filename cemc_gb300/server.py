@@ -1,9 +1,10 @@
 """Continuous-batching Monte Carlo job server on one GPU.
 
 The reference is a single-process library with no server; this module is the
-serving layer the batched kernels make possible.  Jobs (supercell, cluster
-recipe, ECIs, ensemble, temperature, chemical potential, sweep budget) arrive
-at any time.  Jobs that share a geometry (supercell size and cluster set)
+serving layer the batched kernels make possible.  Jobs (a supercell and
+cluster set -- one of the built-in recipes or the job's own settings object --,
+ECIs, ensemble, a temperature / chemical-potential schedule, sweep budgets)
+arrive at any time.  Jobs that share a geometry (supercell size and cluster set)
 share a device-resident slot batch; each batch advances all of its occupied
 slots by one quantum in ONE launch of the fused kernel on its own CUDA
 stream, so batches of different geometries overlap on the device.  A job is
@@ -22,9 +23,17 @@ job's launches split its trials the same way alone or in any mix.
 A job's trials depend only on (seed, job key, trial index) and on its own
 state, and every quantum ends with the same FP64 recompute, so a job's result
 is the same whether it runs alone or in a mix (tested).
+
+Device memory is budgeted: every geometry's tables (their exact size from the
+library), every batch's slots (occupations, site lists, correlation
+functions, ECIs, running sums), its recompute scratch and its conflict tables
+count against ``hbm_budget_gb``.  A job whose batch or geometry does not fit
+waits; batches without jobs are released (least recently used first, with
+their geometry when no other batch uses it) when a waiting job needs the room.
 """
 from __future__ import annotations
 
+import hashlib
 import itertools
 import math
 import threading
@@ -56,6 +65,14 @@ class Job:
     ``occ`` (species ids) defaults to a random configuration at ``composition``
     (fractions per species, default equal); ``eci`` defaults to the seeded
     recipe ECIs; ``mu`` is folded into ``c1_0`` for semi-grand-canonical jobs.
+
+    ``settings``: the job's own settings object (anything ``tables.CEModel``
+    accepts: the CLEASE-style attributes the reference's CE updater reads),
+    used instead of the built-in recipe; ``eci`` is then required and names
+    the cluster set.  ``schedule``: a list of (sweeps, T, mu) segments run one
+    after the other (annealing, chemical-potential scans); it replaces
+    ``sweeps``, ``T`` and ``mu``, and the result carries the averages of each
+    segment under ``"segments"``.
     """
 
     L: int
@@ -68,6 +85,8 @@ class Job:
     eci: Optional[Dict[str, float]] = None
     occ: Optional[np.ndarray] = None
     composition: Optional[List[float]] = None
+    settings: Optional[object] = None
+    schedule: Optional[List[Tuple[float, float, float]]] = None
     job_id: int = -1
     arrival: float = 0.0
     admitted: float = float("nan")
@@ -77,6 +96,26 @@ class Job:
     @property
     def latency(self) -> float:
         return self.done - self.arrival
+
+    def segments(self) -> List[Tuple[float, float, float]]:
+        if self.schedule:
+            return [(float(sw), float(T), float(mu)) for sw, T, mu in self.schedule]
+        return [(float(self.sweeps), float(self.T), float(self.mu))]
+
+
+def group_bytes(geo: E.Geometry, model: CEModel, move: int, capacity: int) -> int:
+    """Device bytes of a batch of ``capacity`` slots: per slot the occupation, (swaps) the site
+    lists, correlation functions and ECIs, energy, temperature, trial counter, status, key,
+    trial budget and running sums; the batch's recompute scratch; exact conflict tables for
+    supercells above ``engine.STAMP_GLOBAL_SITES``."""
+    n = model.n_sites
+    per_slot = n + (8 * n if move == E.MOVE_SWAP else 0) + 16 * model.n_eci + 8 * E.ACCUM_DOUBLES + 48
+    if move == E.MOVE_SWAP:
+        per_slot += 8 * model.n_sym
+    total = capacity * per_slot + 8 * max(geo.scratch_doubles(capacity), 1)
+    if n > E.STAMP_GLOBAL_SITES:
+        total += 4 * geo.stamp_words(capacity)
+    return int(total)
 
 
 class _Group:
@@ -95,9 +134,13 @@ class _Group:
         with torch.cuda.stream(self.stream):
             self.cb = E.ChainBatch(geo, occ, np.zeros(model.n_eci), 1.0, move, seed=server.seed, stream=self.stream)
         self.jobs: List[Optional[Job]] = [None] * capacity
-        self.remaining = np.zeros(capacity, dtype=np.int64)
+        self.remaining = np.zeros(capacity, dtype=np.int64)  # trials left in each slot's current segment
+        self.seg = np.zeros(capacity, dtype=np.int64)        # index of each slot's current segment
+        self.base_eci: List[Optional[np.ndarray]] = [None] * capacity
+        self.seg_results: List[list] = [[] for _ in range(capacity)]
+        self.last_used = time.perf_counter()
         self.chain_trials = torch.zeros(capacity, dtype=torch.int64, device=geo.device)
-        self.bytes_per_slot = n * (1 + (8 if move == E.MOVE_SWAP else 0)) + model.n_eci * 16 + 256
+        self.bytes = group_bytes(geo, model, move, capacity)
         self.launched = False
         self.inflight = False
         self.ev_done = torch.cuda.Event()
@@ -152,6 +195,8 @@ class MCServer:
         self.t_start = None
         self.quantum_trials = int(quantum_trials)
         self.pair_sites = int(pair_sites)
+        self.peak_used = 0.0
+        self._settings_keys: Dict[int, tuple] = {}
 
     # -- submission ------------------------------------------------------------------
     def submit(self, job: Job) -> Job:
@@ -163,20 +208,73 @@ class MCServer:
             self.pending.append(job)
         return job
 
+    def _model_key(self, job: Job):
+        if job.settings is None:
+            return (job.L, job.recipe)
+        key = self._settings_keys.get(id(job.settings))
+        if key is None:
+            if job.eci is None:
+                raise ValueError("a job with its own settings needs its ECIs")
+            m = CEModel(job.settings, list(job.eci))
+            h = hashlib.sha1()
+            for arr in (m.gpu_table, m.term_eci, m.term_ref, m.term_size, m.term_nb, m.bf, m.eci_weight):
+                h.update(np.ascontiguousarray(arr).tobytes())
+            h.update(("|".join(m.eci_names) + "#" + "|".join(m.symbols)).encode())
+            key = ("settings", h.hexdigest())
+            self._settings_keys[id(job.settings)] = key
+            self._built = (key, m, job.settings)  # reused by _model below
+        return key
+
     def _model(self, job: Job):
-        key = (job.L, job.recipe)
+        """The job's model and device geometry (built on first use); None while it does not fit the budget."""
+        key = self._model_key(job)
         hit = self.models.get(key)
         if hit is None:
-            ps, ts, qs, species = RECIPES[job.recipe]
-            s = fcc_settings(job.L, ps, ts, qs, list(species))
-            eci = seeded_ecis(s.cset, 0)
-            m = CEModel(s, list(eci))
+            built = getattr(self, "_built", None)
+            if built is not None and built[0] == key:
+                m, eci = built[1], dict(job.eci)
+                self._built = None
+            elif job.settings is not None:
+                m, eci = CEModel(job.settings, list(job.eci)), dict(job.eci)
+            else:
+                ps, ts, qs, species = RECIPES[job.recipe]
+                s = fcc_settings(job.L, ps, ts, qs, list(species))
+                eci = seeded_ecis(s.cset, 0)
+                m = CEModel(s, list(eci))
             geo = E.Geometry(m, self.device)
-            tbytes = m.n_sites * m.gpu_n_cols * 8 + m.n_terms * 16
-            self.used += tbytes
-            hit = (m, geo, eci)
+            nbytes = geo.device_bytes()
+            if nbytes + group_bytes(geo, m, E.MOVE_FLIP, 1) > self.budget:
+                geo.close()
+                raise MemoryError("the job's geometry does not fit the device-memory budget")
+            if self.used + nbytes > self.budget and not self._release_idle(nbytes):
+                geo.close()
+                return None
+            self._account(nbytes)
+            hit = (m, geo, eci, job.settings)
             self.models[key] = hit
-        return hit
+        return hit[:3]
+
+    def _account(self, nbytes: float):
+        self.used += nbytes
+        self.peak_used = max(self.peak_used, self.used)
+
+    def _release_idle(self, need: float) -> bool:
+        """Free batches without jobs (least recently used first), and geometries no batch uses, until
+        ``need`` more bytes fit the budget; True when they do."""
+        idle = sorted((g for g in self.groups.values() if not g.active() and not g.inflight),
+                      key=lambda g: g.last_used)
+        for grp in idle:
+            if self.used + need <= self.budget:
+                break
+            del self.groups[grp.key]
+            self.used -= grp.bytes
+            gkey = grp.key[:-1]
+            grp.cb = None
+            if not any(k[:-1] == gkey for k in self.groups):
+                m, geo, _, _ = self.models.pop(gkey)
+                self.used -= geo.device_bytes()
+                geo.close()
+        return self.used + need <= self.budget
 
     def _capacity(self, m: CEModel) -> int:
         return int(min(self.capacity, max(4, (1 << 20) // m.n_sites)))
@@ -185,7 +283,8 @@ class MCServer:
         """Build the geometries the given jobs need ahead of time (a warm server); returns seconds."""
         t0 = time.perf_counter()
         for job in jobs:
-            self._model(job)
+            if self._model(job) is None:
+                break
         torch.cuda.synchronize()
         return time.perf_counter() - t0
 
@@ -201,27 +300,48 @@ class MCServer:
             occ = np.repeat(np.arange(m.n_sym, dtype=np.int8), counts)
             rng.shuffle(occ)
         eci = dict(default_eci if job.eci is None else job.eci)
-        if job.ensemble == "sgc":
-            eci["c1_0"] = eci.get("c1_0", 0.0) - job.mu
         return occ, m.eci_vector(eci)
+
+    def _segment_eci(self, grp: _Group, slot: int, mu: float) -> np.ndarray:
+        ev = grp.base_eci[slot].copy()
+        if grp.jobs[slot].ensemble == "sgc":
+            ev[grp.model.eci_names.index("c1_0")] -= mu  # sgc_montecarlo.py:239-261
+        return ev
 
     def _admit(self):
         """Place pending jobs (arrival order) into free slots while memory allows."""
         with self._lock:
             pending = list(self.pending)
         admitted = []
+        rejected = []
         for job in pending:
-            m, geo, eci0 = self._model(job)
+            try:
+                hit = self._model(job)
+            except MemoryError as exc:  # can never run within the budget: hand it back with the reason
+                job.result = {"error": str(exc)}
+                job.admitted = job.done = time.perf_counter()
+                rejected.append(job)
+                continue
+            if hit is None:
+                continue  # its geometry does not fit yet
+            m, geo, eci0 = hit
             move = E.MOVE_FLIP if job.ensemble == "sgc" else E.MOVE_SWAP
-            gkey = (job.L, job.recipe, move)
+            gkey = self._model_key(job) + (move,)
             grp = self.groups.get(gkey)
             if grp is None:
-                need = self._capacity(m) * (m.n_sites * (9 if move == E.MOVE_SWAP else 1) + m.n_eci * 16 + 256)
-                if self.used + need > self.budget:
+                need = group_bytes(geo, m, move, self._capacity(m))
+                if need + geo.device_bytes() > self.budget:
+                    job.result = {"error": "the job's batch does not fit the device-memory budget"}
+                    job.admitted = job.done = time.perf_counter()
+                    rejected.append(job)
+                    continue
+                if self.used + need > self.budget and not self._release_idle(need):
+                    continue
+                if gkey[:-1] not in self.models:  # the release took this job's own idle geometry
                     continue
                 grp = _Group(self, gkey, m, geo, move, self._capacity(m))
                 self.groups[gkey] = grp
-                self.used += need
+                self._account(grp.bytes)
             slot = grp.free_slot()
             if slot < 0:
                 continue
@@ -229,18 +349,24 @@ class MCServer:
             self._load_slot(grp, slot, job, occ, ev)
             job.admitted = time.perf_counter()
             admitted.append(job)
-        if admitted:
+        if admitted or rejected:
+            self.finished.extend(rejected)
             with self._lock:
-                ids = {j.job_id for j in admitted}
+                ids = {j.job_id for j in admitted + rejected}
                 self.pending = [j for j in self.pending if j.job_id not in ids]
 
     def _load_slot(self, grp: _Group, slot: int, job: Job, occ: np.ndarray, ev: np.ndarray):
         cb = grp.cb
         m = grp.model
+        grp.jobs[slot] = job
+        grp.base_eci[slot] = ev
+        grp.seg[slot] = 0
+        grp.seg_results[slot] = []
+        sweeps, T, mu = job.segments()[0]
         with torch.cuda.stream(grp.stream):
             cb.occ[slot].copy_(torch.as_tensor(occ))
-            cb.eci[slot].copy_(torch.as_tensor(ev))
-            cb.kT[slot] = self.kB * job.T
+            cb.eci[slot].copy_(torch.as_tensor(self._segment_eci(grp, slot, mu)))
+            cb.kT[slot] = self.kB * T
             cb.trial[slot] = 0
             # the stream of a job depends on its own seed only, never on its slot or arrival order
             cb.chain_key[slot] = (job.seed * 2654435761 + 97) & 0x7FFFFFFF
@@ -252,8 +378,7 @@ class MCServer:
                 cb.trk_start[slot].copy_(torch.as_tensor(start[0]))
                 cb.trk_count[slot].copy_(torch.as_tensor(count[0]))
         grp.dirty.append(slot)
-        grp.jobs[slot] = job
-        grp.remaining[slot] = int(round(job.sweeps * m.n_sites))
+        grp.remaining[slot] = max(1, int(round(sweeps * m.n_sites)))
 
     # -- the loop ----------------------------------------------------------------------
     def _launch(self, grp: _Group):
@@ -266,6 +391,7 @@ class MCServer:
                 grp.cb.accum[idx] = 0.0
                 grp.cb.accum[idx, E.A_EREF] = grp.cb.energy[idx]
             grp.dirty = []
+        grp.last_used = time.perf_counter()
         per = np.minimum(grp.remaining, grp.quantum)
         per[[j is None for j in grp.jobs]] = 0
         n_max = int(per.max())
@@ -301,29 +427,49 @@ class MCServer:
                 launched.append(grp)
         return launched
 
+    def _segment_result(self, grp: _Group, i: int, acc, energy, cf, kT, sweeps, mu) -> dict:
+        a = acc[i]
+        n = max(a[E.A_NSAMP], 1.0)
+        mean = a[E.A_EREF] + a[E.A_SUM_E] / n
+        T = kT[i] / self.kB
+        return {"temperature": T, "mu": mu, "sweeps": sweeps, "energy": mean, "final_energy": float(energy[i]),
+                "heat_capacity": (a[E.A_SUM_E2] / n - (a[E.A_SUM_E] / n) ** 2) / (self.kB * T * T),
+                "singlet_c1_0": a[E.A_SUM_S] / n, "accept_rate": a[E.A_NACC] / n, "n_mc_steps": int(a[E.A_NSAMP]),
+                "cf": cf[i].copy()}
+
     def _retire(self, groups: List[_Group]):
+        """After a batch's launch: close finished segments, start the next one, hand out finished jobs."""
         for grp in groups:
             grp.stream.synchronize()
             grp.cb.check_status()
-            done = [i for i, j in enumerate(grp.jobs) if j is not None and grp.remaining[i] <= 0]
-            if not done:
+            ends = [i for i, j in enumerate(grp.jobs) if j is not None and grp.remaining[i] <= 0]
+            if not ends:
                 continue
             acc = grp.cb.accum_host()
             energy = grp.cb.energy.cpu().numpy()
             cf = grp.cb.cf.cpu().numpy()
             kT = grp.cb.kT.cpu().numpy()
             now = time.perf_counter()
-            for i in done:
+            for i in ends:
                 job = grp.jobs[i]
-                a = acc[i]
-                n = max(a[E.A_NSAMP], 1.0)
-                mean = a[E.A_EREF] + a[E.A_SUM_E] / n
-                T = kT[i] / self.kB
-                job.result = {"energy": mean, "final_energy": float(energy[i]),
-                              "heat_capacity": (a[E.A_SUM_E2] / n - (a[E.A_SUM_E] / n) ** 2) / (self.kB * T * T),
-                              "singlet_c1_0": a[E.A_SUM_S] / n, "accept_rate": a[E.A_NACC] / n,
-                              "n_mc_steps": int(a[E.A_NSAMP]), "cf": cf[i].copy(),
-                              "occupation": grp.cb.occ[i].cpu().numpy().copy()}
+                segs = job.segments()
+                k = int(grp.seg[i])
+                res = self._segment_result(grp, i, acc, energy, cf, kT, segs[k][0], segs[k][2])
+                grp.seg_results[i].append(res)
+                if k + 1 < len(segs):
+                    # next segment: its temperature and chemical potential, fresh running sums
+                    sweeps, T, mu = segs[k + 1]
+                    grp.seg[i] = k + 1
+                    grp.remaining[i] = max(1, int(round(sweeps * grp.model.n_sites)))
+                    with torch.cuda.stream(grp.stream):
+                        grp.cb.kT[i] = self.kB * T
+                        grp.cb.eci[i].copy_(torch.as_tensor(self._segment_eci(grp, i, mu)))
+                    grp.dirty.append(i)
+                    continue
+                job.result = dict(res)
+                job.result["occupation"] = grp.cb.occ[i].cpu().numpy().copy()
+                if job.schedule:
+                    job.result["segments"] = grp.seg_results[i]
                 job.done = now
                 grp.jobs[i] = None
                 self.finished.append(job)
@@ -364,7 +510,7 @@ class MCServer:
                 "p50_run_s": float(np.percentile(run, 50)), "p99_run_s": float(np.percentile(run, 99)),
                 "trials": self.trials_done,
                 "trials_per_s": self.trials_done / wall if wall > 0 else 0.0, "wall_s": wall,
-                "hbm_used_gb": self.used / 1e9}
+                "hbm_used_gb": self.used / 1e9, "hbm_peak_gb": self.peak_used / 1e9}
 
 
 def poisson_stream(n_jobs: int, rate: float, seed: int = 0, L_range=(4, 32), sweeps_range=(1e2, 1e4),

@@ -108,6 +108,11 @@ typedef struct cemc_geometry cemc_geometry;
 int cemc_geometry_create(const cemc_geometry_desc *desc, cemc_geometry **out);
 int cemc_geometry_destroy(cemc_geometry *geo);
 
+/* Bytes of device memory the geometry's tables hold (the one allocation
+ * cemc_geometry_create makes), for callers that budget device memory.  No
+ * reference counterpart (the reference keeps its tables in host memory). */
+size_t cemc_geometry_device_bytes(const cemc_geometry *geo);
+
 /* Ensembles of a trial move. */
 #define CEMC_MOVE_FLIP 0  /* semi-grand-canonical single-site flip (sgc_montecarlo.py:62-76) */
 #define CEMC_MOVE_SWAP 1  /* canonical two-site swap (montecarlo.py:890-908) */

@@ -201,6 +201,59 @@ def test_server_result_same_alone_and_in_a_mix(torch_cuda):
         assert j.result["n_mc_steps"] == int(round(j.sweeps * (4 * j.L ** 3)))
 
 
+def test_server_budget_binds_with_schedules_and_own_settings(torch_cuda):
+    """A device-memory budget that holds one batch at a time: jobs of other batches wait, idle batches
+    (and their geometries) are released for them, memory use never exceeds the budget, and every result
+    -- a job with its own settings object (a BCC cell) and a two-segment T / mu schedule among them --
+    equals the job's result alone on an unconstrained server."""
+    from cemc_gb300.lattice import cubic_settings, seeded_ecis
+    from cemc_gb300.server import Job, MCServer, group_bytes
+    bcc = cubic_settings("bcc", 4, 3, 2, 0, ["Al", "Mg"])
+    bcc_eci = dict(seeded_ecis(bcc.cset, 1))
+
+    def jobs():
+        return [Job(L=4, recipe="binary", ensemble="sgc", T=900.0, mu=0.02, sweeps=20, seed=1),
+                Job(L=4, recipe="binary", ensemble="canonical", T=700.0, sweeps=15, seed=2),
+                Job(L=0, settings=bcc, eci=bcc_eci, ensemble="sgc", schedule=[(10, 1200.0, 0.0), (12, 500.0, 0.05)],
+                    seed=3),
+                Job(L=6, recipe="binary", ensemble="sgc", T=800.0, sweeps=10, seed=4)]
+
+    kw = dict(capacity=4, quantum_sweeps=3.0, quantum_trials=1)
+    alone = []
+    for j in jobs():
+        srv = MCServer(hbm_budget_gb=8.0, **kw)
+        srv.submit(j)
+        srv.run_until_idle()
+        alone.append(j)
+    probe = MCServer(hbm_budget_gb=8.0, **kw)
+    sizes = []
+    for j in jobs():
+        m, geo, _ = probe._model(j)
+        move = 0 if j.ensemble == "sgc" else 1
+        sizes.append(geo.device_bytes() + group_bytes(geo, m, move, probe._capacity(m)))
+    big = int(np.argmax(sizes))
+    budget = 1.02 * sizes[big]
+    assert budget < sizes[big] + min(sizes[:big] + sizes[big + 1:])  # the largest batch only fits alone
+    srv = MCServer(hbm_budget_gb=budget / 1e9, **kw)
+    js = [srv.submit(j) for j in jobs()]
+    srv.run_until_idle()
+    assert len(srv.finished) == 4 and all("error" not in j.result for j in js)
+    assert srv.peak_used <= srv.budget
+    others = [j for k, j in enumerate(js) if k != big]
+    assert js[big].admitted >= max(j.done for j in others)  # it waited until the others' memory was released
+    for a, b in zip(alone, js):
+        assert np.array_equal(a.result["occupation"], b.result["occupation"])
+        assert np.array_equal(a.result["cf"], b.result["cf"])
+        assert a.result["energy"] == b.result["energy"]
+    seg = js[2].result["segments"]
+    assert [round(x["temperature"]) for x in seg] == [1200, 500] and [x["mu"] for x in seg] == [0.0, 0.05]
+    assert [x["n_mc_steps"] for x in seg] == [10 * 128, 12 * 128]
+    small = MCServer(hbm_budget_gb=1e-6, **kw)
+    j = small.submit(jobs()[0])
+    small.run_until_idle()
+    assert "error" in j.result
+
+
 def test_fp32_drift_and_recompute_at_benchmark_size(torch_cuda):
     """64 chains x 16384 sites, FP32 energy changes: incremental cf/energy vs the FP64 recompute after 3 sweeps."""
     import torch
