@@ -496,6 +496,69 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   if (spin_masks.empty()) spin_masks.assign(2, 0u);
   if (spin_shift.empty()) spin_shift.assign(1, 0);
 
+  // Periodic box of cells (DevGeo::box_L): sites ((x * L + y) * L + z) * nb + b, and at every
+  // site the table holds the same (cell offset, basis site) per (b, column) as at cell 0.  Tried
+  // for one translation group without background sites, for each basis count nb <= 8 with N / nb
+  // a cube; every entry of the table and the multiply-high divisions are checked.
+  int box_L = 0, box_nb = 0;
+  uint32_t box_mnb = 0, box_mL = 0;
+  std::vector<uint32_t> box_off;
+  auto umulhi = [](uint32_t a, uint32_t m) { return (uint32_t)(((uint64_t)a * m) >> 32); };
+  auto magic = [](uint32_t dv) { return (uint32_t)((((uint64_t)1 << 32) + dv - 1) / dv); };  // ceil(2^32 / dv)
+  for (int nb = 1; nb <= 8 && box_L == 0 && G == 1 && n_movable == N; ++nb) {
+    if (N % nb) continue;
+    const int cells = N / nb;
+    const int L = (int)std::lround(std::cbrt((double)cells));
+    if ((long long)L * L * L != cells || L > 255) continue;
+    auto decode = [&](int site, int &x, int &y, int &z) {
+      int c = site / nb;
+      z = c % L;
+      c /= L;
+      y = c % L;
+      x = c / L;
+      return site % nb;
+    };
+    auto near = [&](int v) { return 2 * v > L ? v - L : v; };  // minimal image in (-L/2, L/2]
+    std::vector<uint32_t> off((size_t)nb * C);
+    for (int b = 0; b < nb; ++b)
+      for (int c = 0; c < C; ++c) {
+        int x, y, z;
+        const int bb = decode(d->table[(size_t)b * C + c], x, y, z);
+        off[(size_t)b * C + c] = (uint32_t)(near(x) + 128) | ((uint32_t)(near(y) + 128) << 8) |
+                                 ((uint32_t)(near(z) + 128) << 16) | ((uint32_t)bb << 24);
+      }
+    bool ok = true;
+    for (int site = 0; site < N && ok; ++site) {
+      int x, y, z;
+      const int b = decode(site, x, y, z);
+      for (int c = 0; c < C; ++c) {
+        const uint32_t o = off[(size_t)b * C + c];
+        int nx = x + (int)(o & 255u) - 128, ny = y + (int)((o >> 8) & 255u) - 128, nz = z + (int)((o >> 16) & 255u) - 128;
+        nx += nx < 0 ? L : 0;
+        nx -= nx >= L ? L : 0;
+        ny += ny < 0 ? L : 0;
+        ny -= ny >= L ? L : 0;
+        nz += nz < 0 ? L : 0;
+        nz -= nz >= L ? L : 0;
+        if (((nx * L + ny) * L + nz) * nb + (int)(o >> 24) != d->table[(size_t)site * C + c]) {
+          ok = false;
+          break;
+        }
+      }
+    }
+    const uint32_t mnb = nb > 1 ? magic((uint32_t)nb) : 0u, mL = L > 1 ? magic((uint32_t)L) : 0u;
+    for (uint32_t v = 0; ok && nb > 1 && v < (uint32_t)N; ++v) ok = umulhi(v, mnb) == v / (uint32_t)nb;
+    for (uint32_t v = 0; ok && L > 1 && v < (uint32_t)cells; ++v) ok = umulhi(v, mL) == v / (uint32_t)L;
+    if (ok) {
+      box_L = L;
+      box_nb = nb;
+      box_mnb = mnb;
+      box_mL = mL;
+      box_off.swap(off);
+    }
+  }
+  if (box_off.empty()) box_off.assign(1, 0u);
+
   // One device allocation for all tables.
   struct Part {
     const void *src;
@@ -532,6 +595,7 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {f_pairinc.data(), f_pairinc.size() * 4, 0},
       {f_ustart.data(), f_ustart.size() * 4, 0},
       {f_upd.data(), f_upd.size() * 4, 0},
+      {box_off.data(), box_off.size() * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -593,6 +657,11 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   g.site_group = reinterpret_cast<const int8_t *>(base + parts[26].off);
   g.geo_start = reinterpret_cast<const int32_t *>(base + parts[27].off);
   g.group_scale = reinterpret_cast<const double *>(base + parts[28].off);
+  g.box_L = box_L;
+  g.box_nb = box_nb;
+  g.box_mnb = box_mnb;
+  g.box_mL = box_mL;
+  g.box_off = reinterpret_cast<const uint32_t *>(base + parts[35].off);
   g.pm1_minus = -1;
   if (B == 1 && S == 2) {
     if (d->bf[0] == 1.0 && d->bf[1] == -1.0) g.pm1_minus = 1;
@@ -673,6 +742,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (recycle && r->kernel != CEMC_KERNEL_AUTO && r->kernel != CEMC_KERNEL_GENERIC)
     return fail(CEMC_ERR_ARG, "waste recycling runs the generic kernel form");
   if (recycle && r->cluster == 2) return fail(CEMC_ERR_ARG, "waste recycling runs one CTA per chain");
+  if ((r->site_allow || r->frozen || r->accept_first) && r->cluster == 2)
+    return fail(CEMC_ERR_ARG, "move constraints and first-move acceptance run one CTA per chain");
   const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
   if (want_spin && !geo->spin_ok)
     return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1, <= 64 columns and "
@@ -791,6 +862,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   a.frozen = r->frozen;
   a.max_attempts = r->max_attempts > 0 ? r->max_attempts : 10000;
   a.accept_first = r->accept_first != 0;
+  a.cons = constrained ? 1 : 0;
   a.tpw = tpw;
   const int n_cl = use_spin ? geo->spin.n_cl : 0, n_masks = use_spin ? geo->spin.n_masks : 0;
   // Evaluation forms to try, in order: spin, or table then generic (AUTO), or the one asked for.
@@ -861,7 +933,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   bool found = false;
   for (size_t fi = 0; fi < forms.size() && !found; ++fi) {
     form = forms[fi];
-    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && !recycle && 2 * r->n_chains <= geo->n_sms &&
+    if (r->cluster == 2 || (tpw == 1 && r->cluster == 0 && !constrained && 2 * r->n_chains <= geo->n_sms &&
                             (round_cap == 0 || round_cap >= 2 * warps))) {
       cemc::RunArgs x = a;
       cemc::McLayout L2{};

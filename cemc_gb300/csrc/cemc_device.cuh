@@ -64,7 +64,58 @@ struct DevGeo {
   const int8_t *site_group;    // [n_sites]
   const int32_t *geo_start;    // [n_groups + 1] table-form geometry range of each group
   const double *group_scale;   // [n_groups] factor on a site's cluster-ECI changes
+  // Periodic box (0 = none): sites numbered ((x * box_L + y) * box_L + z) * box_nb + b over an
+  // L^3 box of cells with box_nb basis sites, and the table equal to a fixed cell offset and basis
+  // site per (b, column) at every site (checked when the geometry is built).  Then a swap trial
+  // computes its neighbour sites instead of loading the two rows.
+  int box_L, box_nb;
+  uint32_t box_mnb, box_mL;    // ceil(2^32 / d) for d = box_nb, box_L (division by multiply-high, checked)
+  const uint32_t *box_off;     // [box_nb * n_cols] (dx + 128) | (dy + 128) << 8 | (dz + 128) << 16 | b' << 24
 };
+
+// A neighbour row: in memory (the table, or a row copied to shared memory), or
+// computed from the site's cell in a periodic box.
+struct RowRef {
+  const int32_t *row;  // nullptr: computed
+  int cx, cy, cz, b;
+};
+__device__ __forceinline__ RowRef row_mem(const int32_t *row) {
+  RowRef r;
+  r.row = row;
+  r.cx = r.cy = r.cz = r.b = 0;
+  return r;
+}
+__device__ __forceinline__ RowRef row_of_site(const DevGeo &g, int site) {
+  RowRef r;
+  if (g.box_L == 0) {
+    r.row = g.table + (size_t)site * g.cpad;
+    r.cx = r.cy = r.cz = r.b = 0;
+    return r;
+  }
+  r.row = nullptr;
+  const uint32_t L = (uint32_t)g.box_L;
+  const uint32_t cell = g.box_nb == 1 ? (uint32_t)site : __umulhi((uint32_t)site, g.box_mnb);
+  r.b = site - (int)(cell * (uint32_t)g.box_nb);
+  const uint32_t q = L == 1 ? cell : __umulhi(cell, g.box_mL);
+  r.cz = (int)(cell - q * L);
+  const uint32_t q2 = L == 1 ? q : __umulhi(q, g.box_mL);
+  r.cy = (int)(q - q2 * L);
+  r.cx = (int)q2;
+  return r;
+}
+__device__ __forceinline__ int row_at(const DevGeo &g, const RowRef &r, int c) {
+  if (r.row) return r.row[c];
+  const uint32_t o = __ldg(g.box_off + r.b * g.n_cols + c);
+  const int L = g.box_L;
+  int x = r.cx + (int)(o & 255u) - 128, y = r.cy + (int)((o >> 8) & 255u) - 128, z = r.cz + (int)((o >> 16) & 255u) - 128;
+  x += x < 0 ? L : 0;
+  x -= x >= L ? L : 0;
+  y += y < 0 ? L : 0;
+  y -= y >= L ? L : 0;
+  z += z < 0 ? L : 0;
+  z -= z >= L ? L : 0;
+  return ((x * L + y) * L + z) * g.box_nb + (int)(o >> 24);
+}
 
 // Ints of one group's block of lane-chunk tables in shared memory:
 // [33] chunk bounds, [32] first ECI per lane, [2 n_eci] lane range per ECI.
@@ -187,13 +238,13 @@ __device__ __forceinline__ int barker(R de, uint32_t ua, uint32_t ub, double kT)
 template <typename R>
 __device__ __forceinline__ void gather_vals(const DevGeo &g, const int8_t *occ, const R *bf_s, int site, int old_s,
                                             int new_s, int ovr_site, int ovr_s, R *vals, int (&nbr)[4], int lane) {
-  const int32_t *row = g.table + (size_t)site * g.cpad;
+  const RowRef row = row_of_site(g, site);
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int c = lane + 32 * j;
     nbr[j] = -1;
     if (c < g.n_cols) {
-      const int s = __ldg(row + c);
+      const int s = row_at(g, row, c);
       nbr[j] = s;
       const int o = (s == ovr_site) ? ovr_s : (int)occ[s];
       for (int d = 0; d < g.n_bf; ++d) vals[c * g.n_bf + d] = bf_s[d * g.n_sym + o];

@@ -37,6 +37,7 @@ struct RunArgs {
   const uint32_t *frozen;
   int max_attempts;
   int accept_first;  // the first trial of the call (chunk offset 0) is accepted whatever its energy change
+  int cons;          // 1: the build with the constraint redraw loop and first-move acceptance (one CTA per chain)
 };
 
 constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two or three more warps are helpers

@@ -102,18 +102,18 @@ __device__ __forceinline__ void gather_smem_row(const DevGeo &g, const int8_t *o
 // Spin word of a neighbour row (binary +1/-1 basis): bit c = 1 when column c
 // holds the -1 species; one ballot per 32 columns.  `ovr_site` reads as spin
 // bit `ovr_bit` (the first half of a swap already applied).
-__device__ __forceinline__ void spin_ballot(const DevGeo &g, const int8_t *occ, const int32_t *row, uint32_t xorv,
+__device__ __forceinline__ void spin_ballot(const DevGeo &g, const int8_t *occ, const RowRef &row, uint32_t xorv,
                                             int ovr_site, uint32_t ovr_bit, uint32_t &lo, uint32_t &hi,
                                             int (&nbr)[4], int lane) {
   uint32_t b0 = 0, b1 = 0;
   nbr[0] = nbr[1] = nbr[2] = nbr[3] = -1;
   if (lane < g.n_cols) {
-    const int s = row[lane];
+    const int s = row_at(g, row, lane);
     nbr[0] = s;
     b0 = (s == ovr_site) ? ovr_bit : ((uint32_t)occ[s] ^ xorv);
   }
   if (lane + 32 < g.n_cols) {
-    const int s = row[lane + 32];
+    const int s = row_at(g, row, lane + 32);
     nbr[1] = s;
     b1 = (s == ovr_site) ? ovr_bit : ((uint32_t)occ[s] ^ xorv);
   }
@@ -149,14 +149,14 @@ __device__ __forceinline__ bool change_legal(const uint8_t *allow, uint32_t froz
 // Species of the neighbour columns of `row` into sp[0..n_cols) (site `ovr` read
 // as species `ovr_s`); each lane keeps the site ids of its columns in nbr[] for
 // the conflict stamps.
-__device__ __forceinline__ void table_gather(const DevGeo &g, const int8_t *occ, const int32_t *row, int ovr,
+__device__ __forceinline__ void table_gather(const DevGeo &g, const int8_t *occ, const RowRef &row, int ovr,
                                              int ovr_s, int8_t *sp, int (&nbr)[4], int lane) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int c = lane + 32 * j;
     nbr[j] = -1;
     if (c < g.n_cols) {
-      const int s = row[c];
+      const int s = row_at(g, row, c);
       nbr[j] = s;
       sp[c] = (int8_t)(s == ovr ? ovr_s : occ[s]);
     }
@@ -229,7 +229,9 @@ __device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
   return (double)hi + (double)lo;
 }
 
-template <typename R, int MOVE, int FORM, int CL, int TPW>
+// CONS: this build runs the move-constraint redraw loop and the first-move acceptance (one
+// trial per warp, one CTA per chain); unconstrained launches take builds without them.
+template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS>
 __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
@@ -435,9 +437,9 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   const double kT = a.kT[chain];
   // move constraints of this chain (the redraw loop runs only when there are any; the half-warp
   // form takes no constraints, and keeping these out of it at compile time keeps its code as fast)
-  const uint8_t *allow = (TPW == 1 && a.site_allow) ? a.site_allow + (size_t)chain * N : nullptr;
-  const uint32_t frz = (TPW == 1 && a.frozen) ? a.frozen[chain] : 0u;
-  const bool cons = allow != nullptr || frz != 0u;
+  const uint8_t *allow = (CONS && a.site_allow) ? a.site_allow + (size_t)chain * N : nullptr;
+  const uint32_t frz = (CONS && a.frozen) ? a.frozen[chain] : 0u;
+  const bool cons = CONS && (allow != nullptr || frz != 0u);
   const float inv_kT = (float)(1.0 / kT);
   const uint32_t key = a.chain_key ? a.chain_key[chain] : (uint32_t)chain;
   uint64_t my_trials = a.n_trials;
@@ -491,8 +493,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           const int A = misc[4 + ia], B = misc[4 + ib];
           const int pa = trk[misc[12 + A] + (int)cemc_below(w0.v[2], (uint32_t)misc[20 + A])];
           const int pb = trk[misc[12 + B] + (int)cemc_below(w0.v[3], (uint32_t)misc[20 + B])];
-          if ((unsigned)pa < (unsigned)N) prefetch_row(g.table + (size_t)pa * cpad, cpad);
-          if ((unsigned)pb < (unsigned)N) prefetch_row(g.table + (size_t)pb * cpad, cpad);
+          if (g.box_L == 0 && (unsigned)pa < (unsigned)N) prefetch_row(g.table + (size_t)pa * cpad, cpad);
+          if (g.box_L == 0 && (unsigned)pb < (unsigned)N) prefetch_row(g.table + (size_t)pb * cpad, cpad);
         }
       } else {
         d.x0 = d.x1 = 0;
@@ -897,12 +899,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             }
             old_a = oa;
             if constexpr (TAB) {
-              table_gather(g, occ, frow, -1, 0, sp_a, nbra, lane);
+              table_gather(g, occ, row_mem(frow), -1, 0, sp_a, nbra, lane);
             } else if constexpr (!SPIN) {
               gather_smem_row<R>(g, occ, bf_s, frow, oa, na, va, nbra, lane);
             } else {
               occ_a_bit = (uint32_t)oa ^ xorv;
-              spin_ballot(g, occ, frow, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+              spin_ballot(g, occ, row_mem(frow), xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
             }
           } else {
             int ia = (int)cemc_below(dr.w0, (uint32_t)n_present);
@@ -936,15 +938,15 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             na = B_;
             // first half: site a takes B; second half: site b takes A with a already changed
             if constexpr (TAB) {
-              table_gather(g, occ, g.table + (size_t)sa * cpad, -1, 0, sp_a, nbra, lane);
-              table_gather(g, occ, g.table + (size_t)sb * cpad, sa, B_, sp_b, nbrb, lane);
+              table_gather(g, occ, row_of_site(g, sa), -1, 0, sp_a, nbra, lane);
+              table_gather(g, occ, row_of_site(g, sb), sa, B_, sp_b, nbrb, lane);
             } else if constexpr (!SPIN) {
               gather_vals<R>(g, occ, bf_s, sa, A_, B_, -1, 0, va, nbra, lane);
               gather_vals<R>(g, occ, bf_s, sb, B_, A_, sa, B_, vb, nbrb, lane);
             } else {
               occ_a_bit = (uint32_t)A_ ^ xorv;
-              spin_ballot(g, occ, g.table + (size_t)sa * cpad, xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
-              spin_ballot(g, occ, g.table + (size_t)sb * cpad, xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
+              spin_ballot(g, occ, row_of_site(g, sa), xorv, -1, 0u, wa_lo, wa_hi, nbra, lane);
+              spin_ballot(g, occ, row_of_site(g, sb), xorv, sa, occ_a_bit ^ 1u, wb_lo, wb_hi, nbrb, lane);
             }
           }
           R de;
@@ -1021,12 +1023,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           int acc = 0;
           if (lane == 0) {
             // accept_first_trial_move_after_reset: the call's first trial is accepted outright
-            const bool first = TPW == 1 && a.accept_first && a.chunk_offset == 0 && t == t_first;
+            const bool first = CONS && a.accept_first && a.chunk_offset == 0 && t == t_first;
             if constexpr (RECYCLE)
               acc = no_move ? 0 : (first ? 1 : barker<R>(de, ua, ub, kT));
             else
               acc = no_move ? 0 : (first ? 1 : metropolis<R>(de, ua, ub, kT, inv_kT));
-            if (no_move) put(&misc[3], 1);  // reported in the status at the end of the launch
+            if (CONS && no_move) put(&misc[3], 1);  // reported in the status at the end of the launch
             put(&r_sa[gidx], (int32_t)sa);
             put(&r_sb[gidx], (int32_t)(SWAP ? sb : na));
             put(&r_acc[gidx], (int8_t)acc);
@@ -1209,7 +1211,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       ac->n_samples += my_trials;
       ac->n_accept += n_acc_total;
     }
-    if (a.status) a.status[chain] = (TPW == 1 && misc[3]) ? CEMC_ERR_NO_MOVE : 0;
+    if (a.status) a.status[chain] = (CONS && misc[3]) ? CEMC_ERR_NO_MOVE : 0;
   }
 }
 
@@ -1218,9 +1220,9 @@ static unsigned block_threads(const RunArgs &a) {
   return (unsigned)((a.warps + n_bookers(a.cl, a.warps, a.tpw) + 1) * 32);
 }
 
-template <typename R, int MOVE, int FORM, int CL, int TPW>
+template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS = false>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
-  auto k = mc_kernel<R, MOVE, FORM, CL, TPW>;
+  auto k = mc_kernel<R, MOVE, FORM, CL, TPW, CONS>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
@@ -1242,7 +1244,7 @@ static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cuda
 
 template <typename R, int MOVE, int FORM>
 static int clusters_t(const RunArgs &a, size_t smem) {
-  auto k = mc_kernel<R, MOVE, FORM, 2, 1>;
+  auto k = mc_kernel<R, MOVE, FORM, 2, 1, false>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_chains * 2));
@@ -1265,6 +1267,7 @@ static int clusters_t(const RunArgs &a, size_t smem) {
 
 template <typename R, int MOVE, int FORM>
 static cudaError_t launch_f(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
+  if (a.cons) return launch_t<R, MOVE, FORM, 1, 1, true>(g, a, smem, st, sd);  // one CTA per chain (host checks)
   return a.cl == 2 ? launch_t<R, MOVE, FORM, 2, 1>(g, a, smem, st, sd) : launch_t<R, MOVE, FORM, 1, 1>(g, a, smem, st, sd);
 }
 
@@ -1290,14 +1293,15 @@ static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t 
 template <typename R>
 static cudaError_t launch_recycle(const DevGeo &g, const RunArgs &a, int move, size_t smem, cudaStream_t st) {
   const SpinDev none{};
-  return move == CEMC_MOVE_SWAP ? launch_t<R, CEMC_MOVE_SWAP, kFormRecycle, 1, 1>(g, a, smem, st, none)
-                                : launch_t<R, CEMC_MOVE_FLIP, kFormRecycle, 1, 1>(g, a, smem, st, none);
+  return move == CEMC_MOVE_SWAP ? launch_t<R, CEMC_MOVE_SWAP, kFormRecycle, 1, 1, true>(g, a, smem, st, none)
+                                : launch_t<R, CEMC_MOVE_FLIP, kFormRecycle, 1, 1, true>(g, a, smem, st, none);
 }
 
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       int form, const SpinDev *spin) {
   // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
-  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP)) return cudaErrorInvalidValue;
+  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP || a.cons)) return cudaErrorInvalidValue;
+  if (a.cons && a.cl != 1) return cudaErrorInvalidValue;
   if (form == kFormSpin && !spin) return cudaErrorInvalidValue;
   if (form == kFormRecycle) {
     if (a.cl != 1 || a.tpw != 1) return cudaErrorInvalidValue;
