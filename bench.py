@@ -277,6 +277,15 @@ def _timed_steps(step, stream, steps: int, warmup: int, local: int):
     return a.elapsed_time(b) * 1e-3, clk.summary()
 
 
+def ternary_shape(m, pair_sites: int = 16384):
+    """(warps, CTAs per chain) of a ternary swap batch in the uneven workload: cells of at least
+    ``pair_sites`` sites take 16 warps on a CTA pair; smaller ones one CTA with about as many trials
+    per round as commit without conflicts (half of n_sites / (2 n_cols sites per swap), 4 .. 16)."""
+    if m.n_sites >= pair_sites:
+        return 16, 2
+    return max(2, min(16, max(4, m.n_sites // (4 * m.n_cols)))), 1
+
+
 def run_ternary(args):
     """Ternary canonical swaps on 256 chains of uneven supercells in one graph launch per step.
 
@@ -310,8 +319,9 @@ def run_ternary(args):
             counts = np.floor(comp * m.n_sites).astype(int)
             counts[0] += m.n_sites - counts.sum()
             occ[c] = rng.permutation(np.repeat(np.arange(3), counts))
+        warps, cluster = ternary_shape(m, args.ternary_pair_sites)
         runners.append(BatchRunner(geo, occ, m.eci_vector(eci), 800.0, E.MOVE_SWAP, seed=7 + int(L),
-                                   precision=E.PREC_F32, warps=args.warps or 16, cluster=args.cluster,
+                                   precision=E.PREC_F32, warps=args.warps or warps, cluster=args.cluster or cluster,
                                    sweeps_per_step=args.sweeps_per_step, recompute_every=1, graph=True,
                                    chain_keys=np.arange(n) + 1000 * int(L)))
     multi = MultiBatchRunner(runners)
@@ -328,8 +338,11 @@ def run_ternary(args):
                                      "n_chains": int(args.ternary_chains), "sizes": "L uniform 4..24",
                                      "groups": len(runners), "sites_total": int(sum(r.n_chains * r.geo.n_sites
                                                                                     for r in runners)),
-                                     "sweeps_per_step": args.sweeps_per_step, "warps_per_cta": args.warps or 16,
-                                     "launch": "one CUDA graph per step, one stream per supercell size"}}))
+                                     "sweeps_per_step": args.sweeps_per_step,
+                                     "shape": "cells of >= %d sites: 16 warps on a CTA pair; smaller: default "
+                                              "width, one CTA" % args.ternary_pair_sites,
+                                     "launch": "one CUDA graph per step, one stream per supercell size, "
+                                               "largest cells launched first"}}))
     return 0
 
 
@@ -695,6 +708,8 @@ def main(argv=None):
                         "chains of uneven size in one graph launch; pt: the 48-replica tempering ladder; "
                         "canonical1: one FP64 canonical chain of 2048 sites")
     p.add_argument("--ternary-chains", type=int, default=256)
+    p.add_argument("--ternary-pair-sites", type=int, default=16384,
+                   help="ternary cells of at least this many sites run on CTA pairs")
     p.add_argument("--recompute-cell", type=int, default=32)
     p.add_argument("--recompute-chains", type=int, default=48)
     p.add_argument("--served-jobs", type=int, default=300)

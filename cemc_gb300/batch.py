@@ -166,11 +166,16 @@ class MultiBatchRunner:
     def n_chains(self) -> int:
         return sum(r.n_chains for r in self.runners)
 
+    def _launch_order(self):
+        """Groups by descending work per chain (longest first): the chains that set the step start
+        before the short ones take the SMs, and the short ones fill the SMs around them."""
+        return sorted(self.runners, key=lambda r: -r.trials_per_step * (2 if r.geo.model.n_sym > 2 else 1))
+
     def _body(self):
         start = torch.cuda.Event()
         start.record(self.stream)
         done = []
-        for r in self.runners:
+        for r in self._launch_order():
             r.stream.wait_event(start)
             with torch.cuda.stream(r.stream):
                 r._step_body(r.recompute_every == 1)

@@ -189,7 +189,8 @@ def test_gpu_tempering_replica_131072_sites(E, oracle_mod):
 def test_gpu_ternary_uneven_graph_matches_oracle(E, oracle_mod):
     """Ternary canonical chains of a 4^3 and a 24^3 cell (256 and 55296 sites; pairs to the 5th shell,
     triplets to the 3rd, the tetrahedron), Dirichlet compositions, stepped together by one CUDA graph
-    with one stream per size as the benchmark does; every chain against the oracle."""
+    with one stream per size, in the benchmark's launch shapes (the large cell on a CTA pair) and
+    launch order; every chain against the oracle."""
     from cemc_gb300.batch import BatchRunner, MultiBatchRunner
     from cemc_gb300.lattice import fcc_settings, seeded_ecis
     from cemc_gb300.tables import CEModel
@@ -207,9 +208,10 @@ def test_gpu_ternary_uneven_graph_matches_oracle(E, oracle_mod):
             counts[0] += m.n_sites - counts.sum()
             occ[c] = rng.permutation(np.repeat(np.arange(3), counts))
         keys = np.arange(n_chains) + 1000 * L
+        warps, cluster = _bench().ternary_shape(m)
         runners.append(BatchRunner(geo, occ, m.eci_vector(eci), 800.0, E.MOVE_SWAP, seed=7 + L,
-                                   precision=E.PREC_F32, warps=16, sweeps_per_step=1, recompute_every=1,
-                                   graph=True, chain_keys=keys))
+                                   precision=E.PREC_F32, warps=warps, cluster=cluster, sweeps_per_step=1,
+                                   recompute_every=1, graph=True, chain_keys=keys))
         cases.append((m, occ, m.eci_vector(eci), keys, 7 + L))
     multi = MultiBatchRunner(runners)
     multi.capture()
