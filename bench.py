@@ -175,6 +175,7 @@ def measured_peak():
 NCU_MC_TRAFFIC_BYTES = 4828672.0
 NCU_MC_IPC_ACTIVE_SM = 2.23
 NCU_SOURCE = "ncu capture of one 10-sweep launch of the same kernel and workload"
+KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field"}
 
 
 def cpu_port_rate(m, occ, ev, Ts, sample_sweeps: float, threads: int, seed: int = 7):
@@ -595,7 +596,8 @@ def run_gpu(args):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             a.record(stream)
-            cb.run(runner.trials_per_step, precision=E.PREC_F32, warps=runner.warps, cluster=runner.cluster)
+            cb.run(runner.trials_per_step, precision=E.PREC_F32, warps=runner.warps, cluster=runner.cluster,
+                   kernel=runner.kernel)
             b.record(stream)
         stream.synchronize()
         kms.append(a.elapsed_time(b))
@@ -663,13 +665,16 @@ def run_gpu(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "sgc_flip_fcc_binary_16x16x16_64chains", "n_sites": m.n_sites,
                        "n_chains": N_CHAINS, "sweeps_per_step": args.sweeps_per_step, "recompute": "fp64 every step",
-                       "warps_per_cta": runner.warps, "ctas_per_chain": runner.cluster, "cuda_graph": True,
+                       "warps_per_cta": runner.warps, "ctas_per_chain": runner.cluster,
+                       "kernel": KERNEL_NAMES.get(int(cb.last_kernel), str(cb.last_kernel)), "cuda_graph": True,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"},
             "gpu_launches": n_launches,
             "clocks": clocks,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": NCU_MC_TRAFFIC_BYTES, "traffic_source": NCU_SOURCE,
-                         "peak_kind": peak_kind, "kernel": "mc_kernel<float, flip>", "kernel_ms": k_ms,
+                         "peak_kind": peak_kind,
+                         "kernel": "field_kernel<float>" if cb.last_kernel == E.KERNEL_FIELD else "mc_kernel<float, flip>",
+                         "kernel_ms": k_ms,
                          "alg_bytes_per_trial": bytes_per_flip,
                          "note": "HBM does not bind: after the first sweep the kernel works from shared memory "
                                  "and L2; the issue bound below is the one that binds"},

@@ -1,10 +1,13 @@
 """Autotuner for the launch shape of the Monte Carlo kernel.
 
-A launch shape is (warps, cluster): evaluating warps per CTA and CTAs per
-chain (1, or a cluster pair of 2 on two SMs).  Trials per round are their
-product.  The best shape depends on the supercell size (conflict probability
-between trials of one round), the cluster set (work per trial), the move type
-and the number of chains sharing the GPU (pairs only pay while SMs are idle).
+A launch shape is (warps, cluster, kernel): evaluating warps per CTA, CTAs per
+chain (1, or a cluster pair of 2 on two SMs) and the kernel form (the
+library's automatic choice, or the local-field form for single-site flips of a
+geometry that has it).  The best shape depends on the supercell size (conflict
+probability between trials of one round), the cluster set (work per trial),
+the move type, the number of chains sharing the GPU (pairs only pay while SMs
+are idle) and the acceptance rate of the chains (the local-field form spends
+its time on accepted flips, the spin forms on every trial).
 ``best_config`` times short runs of the candidate shapes on the caller's batch
 (state restored afterwards) or on a synthetic one and caches the winner in a
 JSON file keyed by those features and the device name.
@@ -23,6 +26,7 @@ from . import engine as E
 
 CANDIDATES = (4, 8, 16, 24, 30)          # warps per CTA, one CTA per chain
 PAIR_CANDIDATES = (8, 16, 24, 30)        # warps per CTA, cluster pairs
+FIELD_CANDIDATES = (16, 28)              # worker warps of the local-field form
 _CACHE_PATH = os.environ.get("CEMC_AUTOTUNE_CACHE",
                              os.path.join(os.path.expanduser("~"), ".cache", "cemc_gb300", "autotune.json"))
 _lock = threading.Lock()
@@ -34,16 +38,18 @@ def _key(geo, move, precision, n_chains) -> str:
     m = geo.model
     # chains only matter up to one per SM
     sms = torch.cuda.get_device_properties(geo.device).multi_processor_count
-    return "|".join(map(str, ("shape", name, m.n_sites, m.gpu_n_cols, m.n_groups, m.n_terms, m.n_eci, move, precision,
+    return "|".join(map(str, ("shape3", name, m.n_sites, m.gpu_n_cols, m.n_groups, m.n_terms, m.n_eci, move, precision,
                               min(int(n_chains), sms))))
 
 
-def candidates(geo, n_chains: int):
-    """(warps, cluster) shapes worth timing for ``n_chains`` chains on this device."""
+def candidates(geo, n_chains: int, move: int = E.MOVE_SWAP):
+    """(warps, cluster, kernel) shapes worth timing for ``n_chains`` chains on this device."""
     sms = torch.cuda.get_device_properties(geo.device).multi_processor_count
-    out = [(w, 1) for w in CANDIDATES]
+    out = [(w, 1, E.KERNEL_AUTO) for w in CANDIDATES]
     if 2 * int(n_chains) <= sms:
-        out += [(w, 2) for w in PAIR_CANDIDATES]
+        out += [(w, 2, E.KERNEL_AUTO) for w in PAIR_CANDIDATES]
+    if move == E.MOVE_FLIP:
+        out += [(w, 1, E.KERNEL_FIELD) for w in FIELD_CANDIDATES]  # skipped where the geometry lacks it
     return out
 
 
@@ -81,7 +87,7 @@ def tune(geo, move: int, precision: int, n_chains: int, shapes=None, sweeps: flo
 
 def tune_on(cb, precision: int, shapes=None, sweeps: float = 0.25) -> Dict[tuple, float]:
     """Trials/s of each shape on the caller's own batch; its state is restored afterwards."""
-    shapes = list(shapes) if shapes is not None else candidates(cb.geo, cb.n_chains)
+    shapes = list(shapes) if shapes is not None else candidates(cb.geo, cb.n_chains, cb.move)
     names = ["occ", "cf", "energy", "trial", "accum"] + (["trk", "loc"] if cb.trk is not None else [])
     torch.cuda.synchronize()  # the batch's own stream may still be writing its state
     snap = {n: getattr(cb, n).clone() for n in names}
@@ -89,34 +95,39 @@ def tune_on(cb, precision: int, shapes=None, sweeps: float = 0.25) -> Dict[tuple
     stream = cb.stream if cb.stream is not None else torch.cuda.current_stream()
     out = {}
     from ._lib import CemcError
-    for w, cl in shapes:
+    for shape in shapes:
+        w, cl, kern = (tuple(shape) + (E.KERNEL_AUTO,))[:3]
         try:
-            cb.run(trials // 4, precision=precision, warps=w, cluster=cl)
+            cb.run(trials // 4, precision=precision, warps=w, cluster=cl, kernel=kern)
         except CemcError as exc:
-            if exc.code == 5:  # this shape does not fit in shared memory
+            # this shape does not fit in shared memory (5), or the form does not apply here (1)
+            if exc.code == 5 or (exc.code == 1 and kern != E.KERNEL_AUTO):
+                for n, t in snap.items():
+                    getattr(cb, n).copy_(t)
                 continue
             raise
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)  # the kernel runs on the batch's stream
-        cb.run(trials, precision=precision, warps=w, cluster=cl)
+        cb.run(trials, precision=precision, warps=w, cluster=cl, kernel=kern)
         e1.record(stream)
         torch.cuda.synchronize()
-        out[(int(w), int(cl))] = cb.n_chains * trials / (e0.elapsed_time(e1) * 1e-3)
+        out[(int(w), int(cl), int(kern))] = cb.n_chains * trials / (e0.elapsed_time(e1) * 1e-3)
         for n, t in snap.items():
             getattr(cb, n).copy_(t)
     torch.cuda.synchronize()
     return out
 
 
-def best_config(geo, move: int, precision: int, n_chains: int, batch=None) -> Tuple[int, int]:
-    """Cached best (warps, cluster) for this geometry/move/precision/chain count; tuned on ``batch`` when given."""
+def best_config(geo, move: int, precision: int, n_chains: int, batch=None) -> Tuple[int, int, int]:
+    """Cached best (warps, cluster, kernel) for this geometry/move/precision/chain count; tuned on ``batch``
+    when given."""
     key = _key(geo, move, precision, n_chains)
     with _lock:
         if key in _mem:
             return _mem[key]
         disk = _load()
-        if key in disk:
+        if key in disk and len(disk[key]) == 3:
             _mem[key] = tuple(int(x) for x in disk[key])
             return _mem[key]
     rates = tune_on(batch, precision) if batch is not None else tune(geo, move, precision, n_chains)
@@ -130,5 +141,6 @@ def best_config(geo, move: int, precision: int, n_chains: int, batch=None) -> Tu
 
 
 def best_warps(geo, move: int, precision: int, n_chains: int, batch=None) -> int:
-    """Warps per CTA of the best shape (``best_config``)."""
-    return best_config(geo, move, precision, n_chains, batch)[0]
+    """Warps per CTA of the best shape among the library's automatic forms (``best_config``)."""
+    w, _, kern = best_config(geo, move, precision, n_chains, batch)
+    return w if kern == E.KERNEL_AUTO else 16

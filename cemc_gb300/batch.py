@@ -36,9 +36,10 @@ class BatchRunner:
             self.cb = ChainBatch(geo, occ, eci, kB * self.temperatures, move, seed=seed, chain_keys=chain_keys,
                                  stream=self.stream)
         self.precision = int(precision)
+        self.kernel = E.KERNEL_AUTO
         if warps == 0:
             from .autotune import best_config
-            warps, cluster = best_config(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
+            warps, cluster, self.kernel = best_config(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
         self.warps = int(warps)
         self.cluster = int(cluster)  # CTAs per chain (0: chosen by the library)
         self.trials_per_step = max(1, int(round(sweeps_per_step * geo.n_sites)))
@@ -52,7 +53,8 @@ class BatchRunner:
         return self.cb.n_chains
 
     def _step_body(self, with_recompute: bool):
-        self.cb.run(self.trials_per_step, precision=self.precision, warps=self.warps, cluster=self.cluster)
+        self.cb.run(self.trials_per_step, precision=self.precision, warps=self.warps, cluster=self.cluster,
+                    kernel=self.kernel)
         if with_recompute and not self.cb.recomputed:
             self.cb.recompute()
 

@@ -450,6 +450,12 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
         for (int q = 0; q < ncl; ++q)
           if ((((uint64_t)spin_eci[q].pair_hi << 32) | spin_eci[q].pair_lo) & bit) add_inc(q, pinc);
         f_pairinc.insert(f_pairinc.end(), {pinc[0], pinc[1]});
+        // Terms at the target through site 0, by cluster slot: those with one other member
+        // are counted together (one mask; the count of -1 products is a popcount), the
+        // others (and repeated single members) toggle one by one with their parity.
+        std::vector<uint64_t> single(ncl, 0);
+        std::vector<uint64_t> multi;
+        std::vector<int> multi_q;
         for (int t = 0; t < n_masks && field_ok; ++t) {
           const uint64_t m = ((uint64_t)spin_masks[2 * t + 1] << 32) | spin_masks[2 * t];
           if (!(m & bit)) continue;
@@ -465,9 +471,23 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
             mj |= (uint64_t)1 << c3;
             cmap.push_back({c, c2, c3});
           }
-          uint32_t w[2] = {0, 0};
-          add_inc(spin_mask_cl[t], w);
-          f_upd.insert(f_upd.end(), {(uint32_t)mj, (uint32_t)(mj >> 32), w[0], w[1]});
+          const int q = spin_mask_cl[t];
+          if (__builtin_popcountll(mj) == 1 && !(single[q] & mj)) {
+            single[q] |= mj;
+          } else {
+            multi.push_back(mj);
+            multi_q.push_back(q);
+          }
+        }
+        // entry {mask lo, mask hi, field increment, word | kind << 1 | members << 8}
+        for (int q = 0; q < ncl && field_ok; ++q)
+          if (single[q])
+            f_upd.insert(f_upd.end(), {(uint32_t)single[q], (uint32_t)(single[q] >> 32), 1u << fshift[q],
+                                       (uint32_t)fword[q] | 2u | ((uint32_t)__builtin_popcountll(single[q]) << 8)});
+        for (size_t e = 0; e < multi.size() && field_ok; ++e) {
+          const int q = multi_q[e];
+          f_upd.insert(f_upd.end(), {(uint32_t)multi[e], (uint32_t)(multi[e] >> 32), 1u << fshift[q],
+                                     (uint32_t)fword[q]});
         }
       }
       f_ustart[C] = (int32_t)(f_upd.size() / 4);

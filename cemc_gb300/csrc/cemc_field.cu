@@ -18,20 +18,23 @@
 // shared-memory atomicAdd per target word applies them.
 //
 // A round of up to 64 trials:
-//   phase A  worker warp w evaluates trials 4w .. 4w + 3 (one lane each) against
-//            the state at the start of the round, records them, and stamps the
-//            neighbourhood of each of its accepted trials with (round, trial)
-//            into the conflict table (atomicMax keeps the earliest trial);
+//   phase A  the worker warps evaluate the round's trials (one lane each) against
+//            the state at the start of the round and record them; for each of
+//            its accepted trials a warp stamps the trial's neighbourhood with
+//            (round, trial) into the conflict table (atomicMax keeps the earliest
+//            trial), records the spin word of the trial's neighbour row and
+//            appends the trial to the round's list of accepted trials;
 //   barrier  every warp finds the committed prefix: trials before the first
 //            one whose site an earlier accepted trial stamped (an exact test:
 //            the neighbour row of a site lists every site sharing a cluster
 //            with it, and the relation is symmetric);
-//   phase B  the committed accepted flips, spread over the workers, update the
-//            counts of their neighbours and their own occupation.  Two
+//   phase B  the committed accepted flips update the counts of their neighbours
+//            and their own occupation, as units of (flip, 32 columns) spread
+//            over the worker warps, one target column per lane.  Two
 //            committed flips never share a cluster (that would have been a
 //            conflict), so their updates commute and read stable spins;
 //   barrier  the next round sees the committed state.
-// A fetcher warp draws the trials and copies their neighbour rows into a
+// Two fetcher warps draw the trials and copy their neighbour rows into a
 // shared-memory ring with cp.async three or more rounds ahead; one or two
 // booker warps fold each finished round into the running sums and the
 // correlation-function changes one round late, as in mc_kernel.
@@ -69,6 +72,7 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
   const int CW = field_round(W);    // trials per round
   const int TW = (CW + W - 1) / W;  // trials a worker warp evaluates per round
   const int NB = CW > 32 ? 2 : 1;   // booker warps
+  constexpr int NF = kFieldFetchers;
   const bool gst = a.gstamp != nullptr;
   const FieldLayout L = field_layout(g, fd.n_cl, fd.pw, fd.n_cnt, fd.n_upd, (int)sizeof(R), a.ring_bits, gst);
   const uint32_t rmask = (1u << a.ring_bits) - 1u;
@@ -77,8 +81,9 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const bool worker = warp < W;
   const bool booker = !worker && warp < W + NB;
-  const bool fetcher = warp == W + NB;
+  const bool fetcher = warp >= W + NB && warp < W + NB + NF;
   const int bq = booker ? warp - W : 0;
+  const int fq = fetcher ? warp - W - NB : 0;
   const int N = g.n_sites, n_eci = g.n_eci, cpad = g.cpad, n_cols = g.n_cols;
   const int PW = fd.pw, NCL = fd.n_cl;
   const uint32_t xorv = (uint32_t)(fd.minus_id ^ 1);  // spin bit = occ ^ xorv (1 = the -1 species)
@@ -104,6 +109,7 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
   int32_t *ustart_s = reinterpret_cast<int32_t *>(smem + L.ustart);
   uint4 *upd_s = reinterpret_cast<uint4 *>(smem + L.upd);
   unsigned char *rec0 = smem + L.rec;
+  int32_t *alist0 = reinterpret_cast<int32_t *>(smem + L.alist);  // [2][kFieldRound + 1], count last
   FieldDraw *draws = reinterpret_cast<FieldDraw *>(smem + L.draws);
   int32_t *rows = reinterpret_cast<int32_t *>(smem + L.rows);
   uint32_t *stamp = gst ? a.gstamp + (size_t)chain * ((size_t)2 << a.stamp_bits)
@@ -143,6 +149,7 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
   if (tid == 0) {
     misc[1] = 0;
     nacc_slot[0] = nacc_slot[1] = 0;
+    alist0[kFieldRound] = alist0[2 * kFieldRound + 1] = 0;
     for (int b = 0; b < CEMC_MAX_BF; ++b)
       s_start[b] = acc_from<A>((b < g.n_bf && g.singlet_eci[b] >= 0) ? a.cf[(size_t)chain * n_eci + g.singlet_eci[b]]
                                                                      : 0.0);
@@ -201,7 +208,7 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
   auto prefetch = [&](uint64_t t0) {
     uint64_t want = t0 + (uint64_t)pf * (uint64_t)CW;
     if (want > t_end) want = t_end;
-    for (uint64_t t = fill_end + lane; t < want; t += 32) {
+    for (uint64_t t = fill_end + (uint64_t)(32 * fq + lane); t < want; t += 32 * NF) {
       const uint32_t slot = (uint32_t)t & rmask;
       const cemc_u32x4 w0 = cemc_trial_draw(a.seed, key, t, 0);
       FieldDraw d;
@@ -297,35 +304,26 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
     dsum = acc_add_x(dsum, warp_sum(acc ? r_ds[gg] : (R)0));
   };
   // Correlation-function changes of the committed accepted trials in this
-  // booker's half: lane q < n_cl sums delta * (K_q - 2 c_q) of cluster slot q,
-  // exact 64-bit integers; the singlet change is the sum of delta.
+  // booker's half (lane j takes trial 32 bq + j): delta * (K_q - 2 c_q) per
+  // cluster slot q, summed over the lanes with one reduction per slot and kept
+  // by lane q as an exact 64-bit integer; the singlet change is the sum of delta.
   long long cfr = 0, sing = 0;
-  int my_k = 0, my_shift = 0, my_word = 0;
-  uint32_t my_mask = 0;
-  if (booker && lane < NCL) {
-    const uint32_t m = fd.slot_meta[lane];
-    my_k = (int)(m & 255u);
-    my_shift = (int)((m >> 8) & 31u);
-    my_word = (int)((m >> 13) & 1u);
-    const int bits = (int)((m >> 16) & 31u);
-    my_mask = bits >= 32 ? 0xffffffffu : ((1u << bits) - 1u);
-  }
   auto book_cf = [&](const unsigned char *rec, int ks) {
     const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
     const int8_t *r_dl = reinterpret_cast<const int8_t *>(rec + L.rec_dl);
     const uint32_t *r_p = reinterpret_cast<const uint32_t *>(rec + L.rec_p);
-    const int lo = 32 * bq;
-    const int hi = ks < lo + 32 ? ks : lo + 32;
-    unsigned am = __ballot_sync(kFull, lo + lane < hi && r_acc[lo + lane]);
-    while (am) {
-      const int jj = lo + __ffs(am) - 1;
-      am &= am - 1;
-      const int dl = r_dl[jj];
-      sing += dl;
-      if (lane < NCL) {
-        const int c = (int)((r_p[2 * jj + my_word] >> my_shift) & my_mask);
-        cfr += (long long)(dl * (my_k - 2 * c));
-      }
+    const int gg = 32 * bq + lane;
+    const bool v = gg < ks && r_acc[gg];
+    if (!__ballot_sync(kFull, v)) return;
+    const int dl = v ? (int)r_dl[gg] : 0;
+    const uint32_t p0 = v ? r_p[2 * gg] : 0u, p1 = v ? r_p[2 * gg + 1] : 0u;
+    sing += (long long)__reduce_add_sync(kFull, dl);
+    for (int q = 0; q < NCL; ++q) {
+      const uint32_t m = meta_s[q];
+      const uint32_t bits = (m >> 16) & 31u;
+      const int c = (int)(((((m >> 13) & 1u) ? p1 : p0) >> ((m >> 8) & 31u)) & ((1u << bits) - 1u));
+      const int tot = __reduce_add_sync(kFull, dl * ((int)(m & 255u) - 2 * c));
+      if (lane == q) cfr += (long long)tot;
     }
   };
   auto book = [&](const unsigned char *rec, int ks, uint64_t tb) {
@@ -361,6 +359,8 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
       R *r_de = reinterpret_cast<R *>(rec + L.rec_de);
       R *r_ds = reinterpret_cast<R *>(rec + L.rec_ds);
       uint32_t *r_p = reinterpret_cast<uint32_t *>(rec + L.rec_p);
+      uint2 *r_sw = reinterpret_cast<uint2 *>(rec + L.rec_sw);
+      int32_t *alist = alist0 + (round & 1) * (kFieldRound + 1);
       // ---- phase A: one lane per trial ---------------------------------------
       int site = 0;
       bool acc = false;
@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
           r_p[2 * gg + 1] = p1;
         }
       }
-      // conflict stamps of this warp's accepted trials: the site and its row
+      // this warp's accepted trials: conflict stamps on the site and its row, the spin word
+      // of the row (the state phase B reads if the trial commits), an entry in the round's list
       unsigned am = __ballot_sync(kFull, acc);
       while (am) {
         const int l = __ffs(am) - 1;
@@ -405,61 +406,55 @@ __global__ void __launch_bounds__(1024, 1) field_kernel(DevGeo g, RunArgs a, Fie
         const int s = __shfl_sync(kFull, site, l);
         const uint32_t mark = (round << 6) | (uint32_t)(63 - gg);
         const int32_t *row = rows + (size_t)((uint32_t)(t0 + (uint64_t)gg) & rmask) * cpad;
-        if (lane < n_cols) atomicMax(&stamp[row[lane]], mark);
-        if (lane + 32 < n_cols) atomicMax(&stamp[row[lane + 32]], mark);
-        if (lane == 0) atomicMax(&stamp[s], mark);
+        const int s0 = lane < n_cols ? row[lane] : -1;
+        const int s1 = lane + 32 < n_cols ? row[lane + 32] : -1;
+        if (s0 >= 0) atomicMax(&stamp[s0], mark);
+        if (s1 >= 0) atomicMax(&stamp[s1], mark);
+        const uint32_t lo = __ballot_sync(kFull, s0 >= 0 && (((uint32_t)occ[s0] ^ xorv) & 1u));
+        const uint32_t hi = __ballot_sync(kFull, s1 >= 0 && (((uint32_t)occ[s1] ^ xorv) & 1u));
+        if (lane == 0) {
+          atomicMax(&stamp[s], mark);
+          r_sw[gg] = make_uint2(lo, hi);
+          alist[atomicAdd(&alist[kFieldRound], 1)] = gg;
+        }
       }
       __syncthreads();  // records and stamps of the round are complete
       if (!active) break;
       const int ks = prefix(round, t0);
-      // ---- phase B: committed accepted flips, spread over the workers ----------
+      // ---- phase B: committed accepted flips as (flip, column half) units --------
       {
-        const bool a0 = lane < ks && r_acc[lane];
-        const bool a1 = lane + 32 < ks && r_acc[lane + 32];
-        const unsigned m0 = __ballot_sync(kFull, a0);
-        const unsigned m1 = __ballot_sync(kFull, a1);
-        const unsigned below = (1u << lane) - 1u;
-        const int n0 = __popc(m0);
-        const int r0 = __popc(m0 & below), r1 = n0 + __popc(m1 & below);
-        unsigned my0 = __ballot_sync(kFull, a0 && (r0 % W) == warp);
-        unsigned my1 = __ballot_sync(kFull, a1 && (r1 % W) == warp);
-        while (my0 | my1) {
-          int gg;
-          if (my0) {
-            gg = __ffs(my0) - 1;
-            my0 &= my0 - 1;
-          } else {
-            gg = 31 + __ffs(my1);
-            my1 &= my1 - 1;
-          }
-          const int j = r_sa[gg];
+        const int na = alist[kFieldRound];  // accepted trials of the round, committed or not
+        if (warp == 0 && lane == 0) alist0[((round + 1) & 1) * (kFieldRound + 1) + kFieldRound] = 0;
+        for (int u = warp; u < 2 * na; u += W) {
+          const int gg = alist[u >> 1], h = u & 1;
+          if (gg >= ks) continue;  // not committed: re-evaluated next round
           const int ns = r_ns[gg];
-          const uint32_t bj = ((uint32_t)(ns ^ 1) ^ xorv) & 1u;  // spin bit of j before the flip
-          const int32_t *row = rows + (size_t)((uint32_t)(t0 + (uint64_t)gg) & rmask) * cpad;
-          const int s0 = lane < n_cols ? row[lane] : -1;
-          const int s1 = lane + 32 < n_cols ? row[lane + 32] : -1;
-          const uint32_t lo = __ballot_sync(kFull, s0 >= 0 && (((uint32_t)occ[s0] ^ xorv) & 1u));
-          const uint32_t hi = __ballot_sync(kFull, s1 >= 0 && (((uint32_t)occ[s1] ^ xorv) & 1u));
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int c = lane + 32 * h;
-            const int target = h ? s1 : s0;
-            if (target >= 0) {
-              const uint2 pi = pairinc_s[c];
-              uint32_t d0 = bj ? 0u - pi.x : pi.x;
-              uint32_t d1 = bj ? 0u - pi.y : pi.y;
-              const int e1 = ustart_s[c + 1];
-              for (int e = ustart_s[c]; e < e1; ++e) {
-                const uint4 u = upd_s[e];
-                const uint32_t par = bj ^ ((uint32_t)__popc((lo & u.x) ^ (hi & u.y)) & 1u);
-                d0 += par ? 0u - u.z : u.z;
-                d1 += par ? 0u - u.w : u.w;
-              }
-              if (d0) atomicAdd(&pc[(size_t)target * PW], d0);
-              if (PW == 2 && d1) atomicAdd(&pc[(size_t)target * PW + 1], d1);
+          const uint32_t bj = ((uint32_t)(ns ^ 1) ^ xorv) & 1u;  // spin bit of the site before the flip
+          const uint32_t bjm = 0u - bj;
+          const uint2 sw = r_sw[gg];
+          const int c = lane + 32 * h;
+          if (c < n_cols) {
+            const int32_t *row = rows + (size_t)((uint32_t)(t0 + (uint64_t)gg) & rmask) * cpad;
+            const int target = row[c];
+            const uint2 pi = pairinc_s[c];
+            uint32_t d0 = bj ? 0u - pi.x : pi.x;
+            uint32_t d1 = bj ? 0u - pi.y : pi.y;
+            const uint32_t xl = sw.x ^ bjm, xh = sw.y ^ bjm;
+            const int e1 = ustart_s[c + 1];
+#pragma unroll 4
+            for (int e = ustart_s[c]; e < e1; ++e) {
+              const uint4 ue = upd_s[e];
+              // kind 1: members - 2 x (members whose spin differs from s_j's); kind 0: +-1 by parity
+              const int odd = __popc(xl & ue.x) + __popc(xh & ue.y);
+              const uint32_t par = bj ^ ((uint32_t)__popc((sw.x & ue.x) ^ (sw.y & ue.y)) & 1u);
+              const uint32_t v = (ue.w & 2u) ? ue.z * (uint32_t)((int)(ue.w >> 8) - 2 * odd) : (par ? 0u - ue.z : ue.z);
+              if (ue.w & 1u) d1 += v;
+              else d0 += v;
             }
+            if (d0) atomicAdd(&pc[(size_t)target * PW], d0);
+            if (PW == 2 && d1) atomicAdd(&pc[(size_t)target * PW + 1], d1);
           }
-          if (lane == 0) occ[j] = (int8_t)ns;
+          if (h == 0 && lane == 0) occ[r_sa[gg]] = (int8_t)ns;
         }
       }
       __syncthreads();  // the next round reads the committed counts and occupation
@@ -558,8 +553,7 @@ static cudaError_t launch_field_t(const DevGeo &g, const RunArgs &a, const Field
   auto k = field_kernel<R>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int nb = field_round(a.warps) > 32 ? 2 : 1;
-  k<<<dim3((unsigned)a.n_chains), dim3((unsigned)((a.warps + nb + 1) * 32)), smem, st>>>(g, a, fd);
+  k<<<dim3((unsigned)a.n_chains), dim3((unsigned)field_threads(a.warps)), smem, st>>>(g, a, fd);
   return cudaGetLastError();
 }
 

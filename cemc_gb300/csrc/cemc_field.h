@@ -36,8 +36,13 @@ constexpr int kFieldRound = 64;     // trials per round (at most; one stamp-slot
 //   pairinc[c]: packed increments of the pair terms that join a changed site j
 //     to the target site row_j[c] (one per pair ECI whose shell holds c);
 //   upd[ustart[c] .. ustart[c+1]): the multi-site terms at target row_j[c] that
-//     contain j, as the mask of their other members in j's column space and the
-//     field increments.  Verified on the host to be the same for every site.
+//     contain j, in j's column space, each {mask lo, mask hi, field increment,
+//     word | kind << 1 | members << 8}: kind 1 counts together the terms of one
+//     cluster ECI with a single other member (mask = those members; after the
+//     flip the count of -1 products changes by members - 2 x the members whose
+//     spin differs from s_j's old spin), kind 0 is one term whose product
+//     toggles with the parity of its other members.  Verified on the host to be
+//     the same at every site.
 struct FieldDev {
   int n_cl, pw, n_cnt, n_upd, minus_id, singlet_eci;
   const int32_t *slot_eci;    // [n_cl]
@@ -51,7 +56,8 @@ struct FieldDev {
 struct FieldLayout {
   size_t cf, eci, w, acc, cfw, coef, kind, misc;
   size_t meta, scoef, cnt, pairinc, ustart, upd;
-  size_t rec, rec_stride, rec_sa, rec_ns, rec_acc, rec_dl, rec_de, rec_ds, rec_p;
+  size_t rec, rec_stride, rec_sa, rec_ns, rec_acc, rec_dl, rec_de, rec_ds, rec_p, rec_sw;
+  size_t alist;  // [2][kFieldRound + 1]: per round parity, the accepted slots and their count
   size_t draws, rows, stamp, pc, occ, total;
 };
 
@@ -98,6 +104,8 @@ __host__ __device__ inline FieldLayout field_layout(const DevGeo &g, int n_cl, i
   r += 4 * S;
   L.rec_p = r;
   r += 4 * S * 2;
+  L.rec_sw = r;  // spin word of an accepted trial's neighbour row at the start of its round
+  r += 4 * S * 2;
   L.rec_de = r;
   r += (size_t)rsize * S;
   L.rec_ds = r;
@@ -111,6 +119,8 @@ __host__ __device__ inline FieldLayout field_layout(const DevGeo &g, int n_cl, i
   L.rec_stride = falign16(r);
   L.rec = o;
   o = falign16(o + 2 * L.rec_stride);
+  L.alist = o;
+  o = falign16(o + 4 * 2 * (S + 1));
   const size_t ring = (size_t)1 << ring_bits;
   L.draws = o;  // FieldDraw (16 bytes) per ring slot
   o = falign16(o + 16 * ring);
@@ -134,9 +144,14 @@ __host__ __device__ inline int field_ring_bits(int cw) {
   return b;
 }
 
-// Trials per round of `warps` worker warps (four per warp, at most kFieldRound).
-__host__ __device__ inline int field_round(int warps) { return warps * 4 < kFieldRound ? warps * 4 : kFieldRound; }
-constexpr int kFieldMaxWarps = 28;  // worker warps; two bookers and a fetcher make 31 warps at most
+// Trials per round of `warps` worker warps: 64, or 32 for a single worker warp.
+__host__ __device__ inline int field_round(int warps) { return warps >= 2 ? kFieldRound : 32; }
+constexpr int kFieldFetchers = 2;   // fetcher warps
+constexpr int kFieldMaxWarps = 28;  // worker warps; two bookers and two fetchers make 32 warps at most
+// Threads of a field_kernel CTA with `warps` worker warps.
+__host__ __device__ inline int field_threads(int warps) {
+  return (warps + (field_round(warps) > 32 ? 2 : 1) + kFieldFetchers) * 32;
+}
 
 cudaError_t launch_field(const DevGeo &g, const RunArgs &a, const FieldDev &fd, int precision, size_t smem,
                          cudaStream_t st);

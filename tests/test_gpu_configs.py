@@ -85,7 +85,7 @@ def test_gpu_headline_sgc64_matches_oracle(E, oracle_mod):
     runner.step()
     runner.synchronize()
     runner.cb.check_status()
-    assert runner.cb.last_kernel in (E.KERNEL_SPIN_HALFWARP, E.KERNEL_SPIN)
+    assert runner.cb.last_kernel in (E.KERNEL_SPIN_HALFWARP, E.KERNEL_SPIN, E.KERNEL_FIELD)
     orc = oracle_mod.Oracle(m)
     n = m.n_sites
     occ_gpu = runner.cb.occ.cpu().numpy()
@@ -104,7 +104,8 @@ def test_gpu_headline_sgc64_matches_oracle(E, oracle_mod):
 
     # traced sweep of all 64 chains from the same start, same warps / CTAs per chain / form as the runner
     cb = E.ChainBatch(geo, occ, ev, KB * Ts, E.MOVE_FLIP, seed=2026, chain_keys=keys)
-    _, acc, de = cb.run(n, precision=E.PREC_F32, warps=runner.warps, cluster=runner.cluster, trace=True)
+    _, acc, de = cb.run(n, precision=E.PREC_F32, warps=runner.warps, cluster=runner.cluster, kernel=runner.kernel,
+                        trace=True)
     cb.recompute()
     _sync()
     assert cb.last_kernel == runner.cb.last_kernel
