@@ -172,10 +172,11 @@ def measured_peak():
 # written per launch (the one-time read of the occupations and the neighbour table after the
 # L2 flush; it does not grow with the sweep count) and warp instructions issued per cycle on
 # the SMs that hold a chain.  They are reported with that source, never as this run's numbers.
-NCU_MC_TRAFFIC_BYTES = 4828672.0
+NCU_MC_TRAFFIC_BYTES = 4820224.0
 NCU_MC_IPC_ACTIVE_SM = 2.23
 NCU_SOURCE = "ncu capture of one 10-sweep launch of the same kernel and workload"
 KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field"}
+KERNEL_CHOICES = {"auto": 0, "generic": 1, "spin": 2, "half": 3, "table": 4, "field": 5}
 
 
 def cpu_port_rate(m, occ, ev, Ts, sample_sweeps: float, threads: int, seed: int = 7):
@@ -542,7 +543,7 @@ def run_gpu(args):
     bytes_per_flip = 5 * m.n_cols + 1
     keys = np.arange(N_CHAINS) + rank * N_CHAINS
     runner = BatchRunner(geo, occ, ev, Ts, E.MOVE_FLIP, seed=2026, precision=E.PREC_F32, warps=args.warps,
-                         cluster=args.cluster,
+                         cluster=args.cluster, kernel=KERNEL_CHOICES[args.kernel],
                          sweeps_per_step=args.sweeps_per_step, recompute_every=1, graph=True, chain_keys=keys)
     stream = runner.stream
     runner.capture()
@@ -703,6 +704,9 @@ def main(argv=None):
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--warps", type=int, default=0, help="evaluating warps per CTA (0 = autotuned with --cluster)")
     p.add_argument("--cluster", type=int, default=0, help="CTAs per chain, 1 or 2 (0 = chosen by the library)")
+    p.add_argument("--kernel", default="auto", choices=sorted(KERNEL_CHOICES),
+                   help="kernel form of the headline batch with --warps given (auto: the library's choice; "
+                        "with --warps 0 the autotuner chooses)")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweeps-per-step", type=float, default=SWEEPS_PER_STEP)

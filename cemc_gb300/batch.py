@@ -26,7 +26,7 @@ class BatchRunner:
     def __init__(self, geo: Geometry, occ, eci, temperatures, move: int, seed: int = 0,
                  precision: int = E.PREC_F32, warps: int = 0, sweeps_per_step: float = 1.0,
                  recompute_every: int = 1, graph: bool = True, chain_keys=None, kB: float = KB_EV,
-                 stream: Optional[torch.cuda.Stream] = None, cluster: int = 0):
+                 stream: Optional[torch.cuda.Stream] = None, cluster: int = 0, kernel: int = E.KERNEL_AUTO):
         self.geo = geo
         self.kB = kB
         self.temperatures = np.broadcast_to(np.asarray(temperatures, dtype=np.float64),
@@ -36,7 +36,7 @@ class BatchRunner:
             self.cb = ChainBatch(geo, occ, eci, kB * self.temperatures, move, seed=seed, chain_keys=chain_keys,
                                  stream=self.stream)
         self.precision = int(precision)
-        self.kernel = E.KERNEL_AUTO
+        self.kernel = int(kernel)
         if warps == 0:
             from .autotune import best_config
             warps, cluster, self.kernel = best_config(geo, move, self.precision, self.cb.n_chains, batch=self.cb)
