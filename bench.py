@@ -175,8 +175,8 @@ def measured_peak():
 NCU_MC_TRAFFIC_BYTES = 4820224.0
 NCU_MC_IPC_ACTIVE_SM = 2.23
 NCU_SOURCE = "ncu capture of one 10-sweep launch of the same kernel and workload"
-KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field"}
-KERNEL_CHOICES = {"auto": 0, "generic": 1, "spin": 2, "half": 3, "table": 4, "field": 5}
+KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field", 6: "spin quarter-warp"}
+KERNEL_CHOICES = {"auto": 0, "generic": 1, "spin": 2, "half": 3, "table": 4, "field": 5, "quarter": 6}
 
 
 def cpu_port_rate(m, occ, ev, Ts, sample_sweeps: float, threads: int, seed: int = 7):
@@ -674,7 +674,8 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": NCU_MC_TRAFFIC_BYTES, "traffic_source": NCU_SOURCE,
                          "peak_kind": peak_kind,
-                         "kernel": "field_kernel<float>" if cb.last_kernel == E.KERNEL_FIELD else "mc_kernel<float, flip>",
+                         "kernel": "field_kernel<float>" if cb.last_kernel == E.KERNEL_FIELD
+                         else "mc_kernel<float, flip, %s>" % KERNEL_NAMES.get(int(cb.last_kernel), ""),
                          "kernel_ms": k_ms,
                          "alg_bytes_per_trial": bytes_per_flip,
                          "note": "HBM does not bind: after the first sweep the kernel works from shared memory "

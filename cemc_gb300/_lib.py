@@ -31,6 +31,7 @@ KERNEL_SPIN = 2
 KERNEL_SPIN_HALFWARP = 3
 KERNEL_TABLE = 4
 KERNEL_FIELD = 5
+KERNEL_SPIN_QUARTER = 6
 MAX_BF = 4
 MAX_GROUPS = 8
 

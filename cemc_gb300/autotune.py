@@ -27,6 +27,7 @@ from . import engine as E
 CANDIDATES = (4, 8, 16, 24, 30)          # warps per CTA, one CTA per chain
 PAIR_CANDIDATES = (8, 16, 24, 30)        # warps per CTA, cluster pairs
 FIELD_CANDIDATES = (16, 28)              # worker warps of the local-field form
+QUARTER_CANDIDATES = (8, 12, 16)         # warps of the quarter-warp spin form (four flips per warp)
 _CACHE_PATH = os.environ.get("CEMC_AUTOTUNE_CACHE",
                              os.path.join(os.path.expanduser("~"), ".cache", "cemc_gb300", "autotune.json"))
 _lock = threading.Lock()
@@ -50,6 +51,7 @@ def candidates(geo, n_chains: int, move: int = E.MOVE_SWAP):
         out += [(w, 2, E.KERNEL_AUTO) for w in PAIR_CANDIDATES]
     if move == E.MOVE_FLIP:
         out += [(w, 1, E.KERNEL_FIELD) for w in FIELD_CANDIDATES]  # skipped where the geometry lacks it
+        out += [(w, 1, E.KERNEL_SPIN_QUARTER) for w in QUARTER_CANDIDATES]
     return out
 
 

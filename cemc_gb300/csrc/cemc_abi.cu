@@ -511,6 +511,29 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
     f_upd.assign(4, 0u);
   }
   if (f_upd.empty()) f_upd.assign(4, 0u);
+  // Quarter-warp form (four flips per warp): cluster ECIs on lanes 0..7, the multi-site terms cut
+  // into 8 lane ranges with the same 6-bit counters; a trial's odd-term count of one cluster ECI
+  // is summed in an 8-bit field of one warp reduction, so no ECI may have more than 255 terms.
+  std::vector<int32_t> qtr_lane_term(9, 0), qtr_lane_first(8, 0);
+  std::vector<uint8_t> qtr_shift;
+  bool qtr_ok = spin_ok && spin_eci.size() <= 8;
+  for (const auto &e : spin_eci) qtr_ok = qtr_ok && e.n_multi <= 255;
+  if (qtr_ok) {
+    const int q = (n_masks + 7) / 8;
+    for (int l = 0; l <= 8; ++l) qtr_lane_term[l] = std::min(l * q, n_masks);
+    qtr_shift.assign(std::max(n_masks, 1), 0);
+    for (int l = 0; l < 8 && qtr_ok; ++l) {
+      const int lo = qtr_lane_term[l], hi = qtr_lane_term[l + 1];
+      if (lo >= hi) continue;
+      qtr_lane_first[l] = spin_mask_cl[lo];
+      for (int t = lo; t < hi; ++t) {
+        const int sl = spin_mask_cl[t] - qtr_lane_first[l];
+        if (sl > 4 || hi - lo > 63) qtr_ok = false;
+        qtr_shift[t] = (uint8_t)(6 * sl);
+      }
+    }
+  }
+  if (qtr_shift.empty()) qtr_shift.assign(1, 0);
   if (half_shift.empty()) half_shift.assign(1, 0);
   if (spin_eci.empty()) spin_eci.push_back(cemc::SpinEci{});
   if (spin_masks.empty()) spin_masks.assign(2, 0u);
@@ -616,6 +639,9 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
       {f_ustart.data(), f_ustart.size() * 4, 0},
       {f_upd.data(), f_upd.size() * 4, 0},
       {box_off.data(), box_off.size() * 4, 0},
+      {qtr_shift.data(), qtr_shift.size(), 0},
+      {qtr_lane_term.data(), 9 * 4, 0},
+      {qtr_lane_first.data(), 8 * 4, 0},
   };
   size_t total = 0;
   for (auto &p : parts) {
@@ -697,6 +723,10 @@ extern "C" int cemc_geometry_create(const cemc_geometry_desc *d, cemc_geometry *
   geo->spin.shift = reinterpret_cast<const uint8_t *>(base + parts[15].off);
   geo->spin.lane_term = reinterpret_cast<const int32_t *>(base + parts[16].off);
   geo->spin.lane_first = reinterpret_cast<const int32_t *>(base + parts[17].off);
+  geo->spin.qtr_ok = qtr_ok ? 1 : 0;
+  geo->spin.qtr_shift = reinterpret_cast<const uint8_t *>(base + parts[36].off);
+  geo->spin.qtr_lane_term = reinterpret_cast<const int32_t *>(base + parts[37].off);
+  geo->spin.qtr_lane_first = reinterpret_cast<const int32_t *>(base + parts[38].off);
   geo->spin.half_ok = half_ok ? 1 : 0;
   geo->spin.half_shift = reinterpret_cast<const uint8_t *>(base + parts[18].off);
   geo->spin.half_lane_term = reinterpret_cast<const int32_t *>(base + parts[19].off);
@@ -754,7 +784,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (r->n_chains > 65535 * 32) return fail(CEMC_ERR_LIMIT, "too many chains in one launch");
   r->kernel_used = CEMC_KERNEL_AUTO;  // nothing launched yet
   if (r->n_trials == 0) return CEMC_OK;
-  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_FIELD)
+  if (r->kernel < CEMC_KERNEL_AUTO || r->kernel > CEMC_KERNEL_SPIN_QUARTER)
     return fail(CEMC_ERR_ARG, "unknown kernel %d", (int)r->kernel);
   if (r->cluster < 0 || r->cluster > 2) return fail(CEMC_ERR_ARG, "cluster must be 0 (auto), 1 or 2");
   // waste recycling runs its own build of the generic form, one CTA per chain
@@ -764,7 +794,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   if (recycle && r->cluster == 2) return fail(CEMC_ERR_ARG, "waste recycling runs one CTA per chain");
   if ((r->site_allow || r->frozen || r->accept_first) && r->cluster == 2)
     return fail(CEMC_ERR_ARG, "move constraints and first-move acceptance run one CTA per chain");
-  const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP;
+  const bool want_spin = r->kernel == CEMC_KERNEL_SPIN || r->kernel == CEMC_KERNEL_SPIN_HALFWARP ||
+                         r->kernel == CEMC_KERNEL_SPIN_QUARTER;
   if (want_spin && !geo->spin_ok)
     return fail(CEMC_ERR_ARG, "the spin-basis kernel needs two species with basis values +1/-1, <= 64 columns and "
                               "one translation-symmetry group");
@@ -776,6 +807,10 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   const bool constrained = r->site_allow != nullptr || r->frozen != nullptr || r->accept_first != 0 || recycle;
   if (r->max_attempts < 0) return fail(CEMC_ERR_ARG, "max_attempts must be >= 0");
   const bool half_ok = use_spin && geo->spin.half_ok && r->move == CEMC_MOVE_FLIP && !constrained;
+  if (r->kernel == CEMC_KERNEL_SPIN_QUARTER &&
+      !(use_spin && geo->spin.qtr_ok && r->move == CEMC_MOVE_FLIP && !constrained && r->cluster != 2))
+    return fail(CEMC_ERR_ARG, "the quarter-warp spin kernel runs unconstrained single-site flips with at most 8 "
+                              "cluster ECIs, one CTA per chain");
   if (r->kernel == CEMC_KERNEL_SPIN_HALFWARP && !half_ok)
     return fail(CEMC_ERR_ARG, "the half-warp spin kernel runs unconstrained single-site flips with at most 16 "
                               "cluster ECIs");
@@ -840,7 +875,8 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   }
   // two trials per warp: asked for, or chosen when eligible and no CTA pair was asked for
   // (a CTA pair takes the half-warp form only when that form is asked for explicitly)
-  const int tpw = (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
+  const int tpw = r->kernel == CEMC_KERNEL_SPIN_QUARTER ? 4 :
+                  (r->kernel == CEMC_KERNEL_SPIN_HALFWARP || (r->kernel == CEMC_KERNEL_AUTO && half_ok &&
                                                                 r->cluster != 2)) ? 2 : 1;
   // Default round width: 16 evaluating warps, fewer where most trials of a
   // round would conflict.  A changed site reaches about n_cols sites, so with
@@ -1004,7 +1040,7 @@ extern "C" int cemc_run(const cemc_geometry *geo, cemc_run_desc *r, void *stream
   }
   r->kernel_used = form == cemc::kFormTable ? CEMC_KERNEL_TABLE
                   : (form == cemc::kFormGeneric || form == cemc::kFormRecycle) ? CEMC_KERNEL_GENERIC
-                  : (a.tpw == 2 ? CEMC_KERNEL_SPIN_HALFWARP : CEMC_KERNEL_SPIN);
+                  : (a.tpw == 4 ? CEMC_KERNEL_SPIN_QUARTER : a.tpw == 2 ? CEMC_KERNEL_SPIN_HALFWARP : CEMC_KERNEL_SPIN);
   if (form == cemc::kFormTable) {
     cudaError_t e = cemc::launch_recompute(g, r->n_chains, r->occ, r->eci, r->cf, r->energy, rscratch,
                                            static_cast<cudaStream_t>(stream));

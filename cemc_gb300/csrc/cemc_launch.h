@@ -52,6 +52,7 @@ __host__ __device__ inline int n_bookers(int cl, int warps, int tpw) {
 }
 // Evaluating warps per CTA that fit next to the helpers in 1024 threads.
 __host__ __device__ inline int max_eval_warps(int cl, int tpw) {
+  if (tpw == 4) return kRoundSlots / 4;                 // four trials per warp, one CTA per chain
   if (tpw == 2) return cl == 1 ? 29 : kRoundSlots / 4;  // a pair of half-warp CTAs: 4 trials per warp index
   return kMaxEval;
 }
@@ -125,7 +126,7 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 16 * (size_t)n_masks);
   L.sp_shift = o;  // (unused)
   L.sp_lane = o;
-  if (n_cl > 0) o = align16(o + 4 * (33 + 32 + 17 + 16));
+  if (n_cl > 0) o = align16(o + 4 * (33 + 32 + 17 + 16 + 9 + 8));
   size_t r = 0;
   L.rec_sa = r;
   r += 4 * S;

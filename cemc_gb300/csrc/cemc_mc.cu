@@ -311,6 +311,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int32_t *sp_lane_first = sp_lane_term + 33;
   int32_t *sp_half_term = sp_lane_first + 32;  // [17]
   int32_t *sp_half_first = sp_half_term + 17;  // [16]
+  int32_t *sp_qtr_term = sp_half_first + 16;   // [9]
+  int32_t *sp_qtr_first = sp_qtr_term + 9;     // [8]
   const uint32_t xorv = SPIN ? (uint32_t)(sd.minus_id ^ 1) : 0u;  // spin bit = occ ^ xorv (1 = the -1 species)
 
   int8_t *occ = a.occ_smem ? reinterpret_cast<int8_t *>(smem + L.occ) : a.occ + (size_t)chain * N;
@@ -393,12 +395,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   if (SPIN) {
     for (int k = tid; k < sd.n_cl; k += blockDim.x) sp_eci[k] = sd.eci[k];
     for (int t = tid; t < sd.n_masks; t += blockDim.x)
-      sp_terms[t] = make_uint4(sd.masks[t].x, sd.masks[t].y, sd.shift[t], TPW == 2 ? sd.half_shift[t] : 0u);
+      sp_terms[t] = make_uint4(sd.masks[t].x, sd.masks[t].y, sd.shift[t],
+                               TPW == 2 ? sd.half_shift[t] : (TPW == 4 ? sd.qtr_shift[t] : 0u));
     for (int i = tid; i < 33; i += blockDim.x) sp_lane_term[i] = sd.lane_term[i];
     for (int i = tid; i < 32; i += blockDim.x) sp_lane_first[i] = sd.lane_first[i];
     if (TPW == 2) {
       for (int i = tid; i < 17; i += blockDim.x) sp_half_term[i] = sd.half_lane_term[i];
       for (int i = tid; i < 16; i += blockDim.x) sp_half_first[i] = sd.half_lane_first[i];
+    }
+    if (TPW == 4) {
+      for (int i = tid; i < 9; i += blockDim.x) sp_qtr_term[i] = sd.qtr_lane_term[i];
+      for (int i = tid; i < 8; i += blockDim.x) sp_qtr_first[i] = sd.qtr_lane_first[i];
     }
   }
   if (a.occ_smem) {
@@ -696,16 +703,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   int sp_tlo = 0, sp_thi = 0, sp_first = 0;  // this lane's range of multi-site terms
   if (SPIN) {
     // two trials per warp: lane l works for trial l / 16 on cluster ECI (and term range) l % 16
-    const int el = (TPW == 2) ? (lane & 15) : lane;
-    sp_tlo = TPW == 2 ? sp_half_term[el] : sp_lane_term[el];
-    sp_thi = TPW == 2 ? sp_half_term[el + 1] : sp_lane_term[el + 1];
-    sp_first = TPW == 2 ? sp_half_first[el] : sp_lane_first[el];
+    // TPW trials per warp: lane l works for trial l / (32 / TPW) on cluster ECI (and term range) l % (32 / TPW)
+    const int el = lane % (32 / TPW);
+    sp_tlo = TPW == 4 ? sp_qtr_term[el] : (TPW == 2 ? sp_half_term[el] : sp_lane_term[el]);
+    sp_thi = TPW == 4 ? sp_qtr_term[el + 1] : (TPW == 2 ? sp_half_term[el + 1] : sp_lane_term[el + 1]);
+    sp_first = TPW == 4 ? sp_qtr_first[el] : (TPW == 2 ? sp_half_first[el] : sp_lane_first[el]);
     if (el < sd.n_cl) {
       sp_e = sp_eci[el];
       sp_coef = coef_s[sp_e.eci];
     }
     sp_multi = __ballot_sync(kFull, el < sd.n_cl && sp_e.n_multi > 0);
-    if (TPW == 2) sp_multi &= 0xFFFFu;
+    if constexpr (TPW >= 2) sp_multi &= (1u << (32 / TPW)) - 1u;
   }
 
   // One round: every warp, whatever its role, meets the round barrier once and
@@ -765,13 +773,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       uint32_t *tab = stamp + ((size_t)(round & 1) << L.stamp_bits);
       DT *dbuf = drow + (size_t)(round & 1) * TPW * W * n_eci;  // this round's change rows
       DT *Dw = dbuf + (size_t)warp * n_eci;
-      if (TPW == 2) {
-        // ---- phase A, two flips per warp: half h = lane / 16 evaluates trial slot 2 warp + h ----
-        if (active && t0 + (uint64_t)(rank * 2 * W + 2 * warp) < t_end) {
-          const int h = lane >> 4, hl = lane & 15;
-          const int gh = rank * 2 * W + 2 * warp + h;  // trial slot in the round (pairs: CTA 1 after CTA 0)
+      if constexpr (TPW >= 2) {
+        // ---- phase A, TPW flips per warp: lane group h = lane / LW evaluates trial slot TPW warp + h ----
+        constexpr int LW = 32 / TPW;      // lanes per trial (16 or 8)
+        constexpr int NJ = 64 / LW;       // column chunks of a neighbour row
+        constexpr int FB = 32 / TPW;      // bits of a trial's field in the shared reductions
+        constexpr uint32_t LMASK = (1u << LW) - 1u;
+        if (active && t0 + (uint64_t)(rank * TPW * W + TPW * warp) < t_end) {
+          const int h = lane / LW, hl = lane % LW;
+          const int gh = rank * TPW * W + TPW * warp + h;  // trial slot in the round (pairs: CTA 1 after CTA 0)
           const uint64_t t = t0 + (uint64_t)gh;
-          const bool has = t < t_end;  // the second half of the last warp may have no trial
+          const bool has = t < t_end;  // the last groups of the last warp may have no trial
           const uint32_t slot = (uint32_t)t & rmask;
           int sa = 0, na = 0, oa = 0;
           uint32_t ua = 0, ub = 0;
@@ -785,14 +797,14 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             ub = dr.w3;
           }
           const uint32_t occ_a_bit = (uint32_t)oa ^ xorv;
-          // spin word of the neighbour row: bit c = column c, from four ballots of
-          // 16 columns (c = hl + 16 j) of which each half keeps its own 16 bits
+          // spin word of the neighbour row: bit c = column c, from NJ ballots of LW
+          // columns (c = hl + LW j) of which each lane group keeps its own LW bits
           const int32_t *row = rows + (size_t)slot * cpad;
-          int nbr[4];
+          int nbr[NJ];
           uint32_t wl = 0, wh = 0;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int c = hl + 16 * j;
+          for (int j = 0; j < NJ; ++j) {
+            const int c = hl + LW * j;
             uint32_t bit = 0;
             nbr[j] = -1;
             if (has && c < g.n_cols) {
@@ -800,25 +812,23 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
               nbr[j] = sn;
               bit = (uint32_t)occ[sn] ^ xorv;
             }
-            const uint32_t chunk = (__ballot_sync(kFull, bit) >> (16 * h)) & 0xFFFFu;
-            if (j == 0) wl = chunk;
-            else if (j == 1) wl |= chunk << 16;
-            else if (j == 2) wh = chunk;
-            else wh |= chunk << 16;
+            const uint32_t chunk = (__ballot_sync(kFull, bit) >> (LW * h)) & LMASK;
+            if (LW * j < 32) wl |= chunk << (LW * j);
+            else wh |= chunk << (LW * j - 32);
           }
           const uint32_t pa = spin_lane_parities<true>(sp_terms, sp_tlo, sp_thi, wl, wh);
-          // odd-parity counts of each multi-site cluster ECI: one reduction serves
-          // both halves (half h's count in bits 16h .. 16h + 15, at most 16 x 63)
+          // odd-parity counts of each multi-site cluster ECI: one reduction serves every
+          // lane group (group h's count in bits FB h .. FB h + FB - 1; at most 255 when FB = 8)
           int my_odd = 0;
           for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
             const int k = __ffs(mm) - 1;
             const int sl = k - sp_first;
             const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
-            const uint32_t tot = __reduce_add_sync(kFull, v << (16 * h));
-            if (hl == k) my_odd = (int)((tot >> (16 * h)) & 0xFFFFu);
+            const uint32_t tot = __reduce_add_sync(kFull, v << (FB * h));
+            if (hl == k) my_odd = (int)((tot >> (FB * h)) & ((1u << FB) - 1u));
           }
           const int delta = occ_a_bit ? 2 : -2;
-          DT *Dh = dbuf + (size_t)(2 * warp + h) * n_eci;  // this CTA's change row of the trial
+          DT *Dh = dbuf + (size_t)(TPW * warp + h) * n_eci;  // this CTA's change row of the trial
           int P = 0;
           if (hl < sd.n_cl) {
             P = sp_e.n_pairs - 2 * (__popc(wl & sp_e.pair_lo) + __popc(wh & sp_e.pair_hi)) + sp_e.n_multi - 2 * my_odd;
@@ -826,7 +836,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           }
           R sum = sp_coef * (R)P;
 #pragma unroll
-          for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+          for (int o = LW / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
           if (sd.singlet_eci >= 0) {
             if (hl == 0 && has) Dh[sd.singlet_eci] = delta;
             sum += coef_s[sd.singlet_eci];
@@ -841,11 +851,11 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             put(&r_de[gh], de);
             put(&r_ds[gh], (R)delta);  // the singlet change (one decoration)
           }
-          acc = __shfl_sync(kFull, acc, 16 * h);
+          acc = __shfl_sync(kFull, acc, LW * h);
           if (acc) {
             const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < NJ; ++j)
               if (nbr[j] >= 0) {
                 uint32_t *p = &tab[(uint32_t)nbr[j] & hmask];
                 atomicMax(p, mark);
@@ -1281,6 +1291,7 @@ static cudaError_t launch_r(const DevGeo &g, const RunArgs &a, int move, size_t 
     return launch_f<R, CEMC_MOVE_SWAP, kFormGeneric>(g, a, smem, st, none);
   }
   if (form == kFormSpin) {
+    if (a.tpw == 4) return launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 1, 4>(g, a, smem, st, *spin);
     if (a.tpw == 2)
       return a.cl == 2 ? launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 2, 2>(g, a, smem, st, *spin)
                        : launch_t<R, CEMC_MOVE_FLIP, kFormSpin, 1, 2>(g, a, smem, st, *spin);
@@ -1300,7 +1311,8 @@ static cudaError_t launch_recycle(const DevGeo &g, const RunArgs &a, int move, s
 cudaError_t launch_mc(const DevGeo &g, const RunArgs &a, int move, int precision, size_t smem, cudaStream_t st,
                       int form, const SpinDev *spin) {
   // two trials per warp: spin flips on one CTA per chain only (checked by the caller)
-  if (a.tpw == 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP || a.cons)) return cudaErrorInvalidValue;
+  if (a.tpw >= 2 && (form != kFormSpin || move != CEMC_MOVE_FLIP || a.cons)) return cudaErrorInvalidValue;
+  if (a.tpw == 4 && a.cl != 1) return cudaErrorInvalidValue;
   if (a.cons && a.cl != 1) return cudaErrorInvalidValue;
   if (form == kFormSpin && !spin) return cudaErrorInvalidValue;
   if (form == kFormRecycle) {

@@ -39,6 +39,12 @@ struct SpinDev {
   const uint8_t *half_shift;       // [n_masks]
   const int32_t *half_lane_term;   // [17]
   const int32_t *half_lane_first;  // [16]
+  // Quarter-warp form (one flip per 8 lanes): the terms cut into 8 lane ranges; usable when
+  // qtr_ok (at most 8 cluster ECIs, at most 255 terms per ECI, counters fit).
+  int qtr_ok;
+  const uint8_t *qtr_shift;       // [n_masks]
+  const int32_t *qtr_lane_term;   // [9]
+  const int32_t *qtr_lane_first;  // [8]
 };
 
 }  // namespace cemc

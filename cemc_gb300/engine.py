@@ -28,6 +28,7 @@ KERNEL_SPIN = _lib.KERNEL_SPIN
 KERNEL_SPIN_HALFWARP = _lib.KERNEL_SPIN_HALFWARP
 KERNEL_TABLE = _lib.KERNEL_TABLE
 KERNEL_FIELD = _lib.KERNEL_FIELD
+KERNEL_SPIN_QUARTER = _lib.KERNEL_SPIN_QUARTER
 STAMP_GLOBAL_SITES = 16384  # larger supercells get exact conflict tables in device memory
 ACCUM_DOUBLES = _lib.ACCUM_DOUBLES
 # Field offsets (in doubles) of cemc_accum.

@@ -214,6 +214,8 @@ typedef struct {
 #define CEMC_KERNEL_FIELD 5  /* local field: spin basis, unconstrained flips of a periodic one-group supercell;
                                 every site keeps its per-ECI odd-term counts in shared memory, a trial reads
                                 them (one lane per trial) and an accepted flip updates its neighbours' counts */
+#define CEMC_KERNEL_SPIN_QUARTER 6  /* spin basis, flips only, four trials per warp (one per 8 lanes), at most 8
+                                       cluster ECIs, one CTA per chain */
 
 /* Run n_trials Metropolis trials on every chain in one launch: trial-move
  * energy change, accept test and in-place commit of occupation, correlation

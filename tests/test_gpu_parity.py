@@ -62,6 +62,12 @@ def _kernel_ok(m, kernel, E, move=0, cluster=0):
         pytest.skip("the half-warp spin kernel runs flips")
     if kernel == E.KERNEL_TABLE and np.any(np.asarray(m.group_scale) != 1.0):
         pytest.skip("the table kernel needs translation groups of equal size")
+    if kernel == E.KERNEL_SPIN_QUARTER:
+        if not (m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0] and m.n_groups == 1
+                and int((np.asarray(m.eci_kind) == 2).sum()) <= 8):
+            pytest.skip("the quarter-warp spin kernel needs a binary +1/-1 basis, one group, <= 8 cluster ECIs")
+        if move != 0 or cluster == 2:
+            pytest.skip("the quarter-warp spin kernel runs flips on one CTA per chain")
     if kernel == E.KERNEL_FIELD:
         if not (m.n_sym == 2 and sorted(m.bf[0].tolist()) == [-1.0, 1.0] and m.n_groups == 1
                 and len(m.movable) == m.n_sites):
@@ -70,7 +76,7 @@ def _kernel_ok(m, kernel, E, move=0, cluster=0):
             pytest.skip("the local-field kernel runs flips on one CTA per chain")
 
 
-KERNELS = [1, 2, 3, 4, 5]  # generic, spin, spin half-warp, table, local field
+KERNELS = [1, 2, 3, 4, 5, 6]  # generic, spin, spin half-warp, table, local field, spin quarter-warp
 CLUSTERS = [1, 2]  # CTAs per chain
 
 
@@ -230,7 +236,7 @@ def test_gpu_batch_equals_oracle_per_chain(move, prec, kernel, cluster, E, oracl
 def test_gpu_launch_splitting_is_invisible(kernel, E):
     """k launches of n/k trials equal one launch of n (counter-based proposals, resident state),
     whatever the launch shape of each piece (warps, CTAs per chain, trials per warp)."""
-    flips_only = kernel in (E.KERNEL_SPIN_HALFWARP, E.KERNEL_FIELD)
+    flips_only = kernel in (E.KERNEL_SPIN_HALFWARP, E.KERNEL_FIELD, E.KERNEL_SPIN_QUARTER)
     g = load_golden("binary_flip" if flips_only else "binary_swap")
     move = 0 if flips_only else 1
     s, m, eci = golden_model(g)
@@ -239,7 +245,7 @@ def test_gpu_launch_splitting_is_invisible(kernel, E):
     b = E.ChainBatch(geo, g["occ0"][None], g["eci"], float(g["kT"]), move, seed=4)
     a.run(3000, precision=0, warps=16, kernel=kernel, cluster=1)
     for i in range(3):
-        if i == 1 and kernel == E.KERNEL_FIELD:  # the middle piece in another kernel form on a CTA pair
+        if i == 1 and kernel in (E.KERNEL_FIELD, E.KERNEL_SPIN_QUARTER):  # another form on a CTA pair
             b.run(1000, precision=0, warps=7, kernel=E.KERNEL_SPIN_HALFWARP, cluster=2)
         elif i == 1:  # the middle piece on a CTA pair
             b.run(1000, precision=0, warps=7, kernel=kernel, cluster=2)
