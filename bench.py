@@ -172,9 +172,10 @@ def measured_peak():
 # written per launch (the one-time read of the occupations and the neighbour table after the
 # L2 flush; it does not grow with the sweep count) and warp instructions issued per cycle on
 # the SMs that hold a chain.  They are reported with that source, never as this run's numbers.
-NCU_MC_TRAFFIC_BYTES = 4820224.0
-NCU_MC_IPC_ACTIVE_SM = 2.23
-NCU_SOURCE = "ncu capture of one 10-sweep launch of the same kernel and workload"
+# Per kernel form (CEMC_KERNEL_* id): (DRAM bytes per launch, IPC per busy SM, launch captured).
+NCU_FIGURES = {3: (4820224.0, 2.23, "one 10-sweep launch"),
+               5: (4820992.0, 2.31, "one 2-sweep launch (traffic does not grow with sweeps)")}
+NCU_SOURCE = "ncu capture of the same kernel and workload: "
 KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field", 6: "spin quarter-warp"}
 KERNEL_CHOICES = {"auto": 0, "generic": 1, "spin": 2, "half": 3, "table": 4, "field": 5, "quarter": 6}
 
@@ -199,15 +200,17 @@ def calibrated_cpu_sample(m, occ, ev, Ts, threads: int, target_s: float):
     return sweeps
 
 
-def correctness_sample(geo, m, occ, ev, Ts, n_trials: int = 40000, chain: int = N_CHAINS - 1):
-    """FP32 energy changes vs the FP64 oracle on one chain of the workload (the hottest, highest-acceptance one)."""
+def correctness_sample(geo, m, occ, ev, Ts, n_trials: int = 40000, chain: int = N_CHAINS - 1, warps: int = 8,
+                       kernel: int = 0):
+    """FP32 energy changes vs the FP64 oracle on one chain of the workload (the hottest, highest-acceptance one),
+    in the timed batch's warps and kernel form."""
     import torch
     from cemc_gb300 import engine as E
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     kT = KB * Ts[chain]
     cb = E.ChainBatch(geo, occ[chain:chain + 1], ev[chain:chain + 1], kT, E.MOVE_FLIP, seed=77)
-    _, acc, de = cb.run(n_trials, precision=E.PREC_F32, warps=8, trace=True)
+    _, acc, de = cb.run(n_trials, precision=E.PREC_F32, warps=warps, kernel=kernel, trace=True)
     torch.cuda.synchronize()
     acc, de = acc.cpu().numpy()[0], de.cpu().numpy()[0]
     orc = O.Oracle(m)
@@ -608,6 +611,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peak()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     busy_sms = min(sms, N_CHAINS * max(1, runner.cluster))
+    ncu_traffic, ncu_ipc, ncu_launch = NCU_FIGURES.get(int(cb.last_kernel), (None, None, None))
 
     # -- end to end through the public batched API, host buffers each step ---------------
     occ_h = torch.from_numpy(occ).pin_memory()
@@ -645,7 +649,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         plain = n_launch * m.n_sites / (time.perf_counter() - t0)
 
-    corr = correctness_sample(geo, m, occ, ev, Ts) if rank == 0 and not args.no_correctness else None
+    corr = (correctness_sample(geo, m, occ, ev, Ts, warps=runner.warps, kernel=runner.kernel)
+            if rank == 0 and not args.no_correctness else None)
 
     # -- CPU baseline on a bounded sample (rank 0) --------------------------------------
     cpu = None
@@ -672,7 +677,8 @@ def run_gpu(args):
             "gpu_launches": n_launches,
             "clocks": clocks,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": NCU_MC_TRAFFIC_BYTES, "traffic_source": NCU_SOURCE,
+                         "frac": achieved / peak, "traffic": ncu_traffic,
+                         "traffic_source": NCU_SOURCE + ncu_launch if ncu_launch else None,
                          "peak_kind": peak_kind,
                          "kernel": "field_kernel<float>" if cb.last_kernel == E.KERNEL_FIELD
                          else "mc_kernel<float, flip, %s>" % KERNEL_NAMES.get(int(cb.last_kernel), ""),
@@ -681,8 +687,8 @@ def run_gpu(args):
                          "note": "HBM does not bind: after the first sweep the kernel works from shared memory "
                                  "and L2; the issue bound below is the one that binds"},
             "issue_bound": {"sms_holding_a_chain": busy_sms, "sms": sms, "sm_fraction": busy_sms / sms,
-                            "ipc_per_busy_sm": NCU_MC_IPC_ACTIVE_SM, "ipc_source": NCU_SOURCE,
-                            "frac_of_gpu_issue": NCU_MC_IPC_ACTIVE_SM * busy_sms / (4.0 * sms)},
+                            "ipc_per_busy_sm": ncu_ipc, "ipc_source": NCU_SOURCE + ncu_launch if ncu_launch else None,
+                            "frac_of_gpu_issue": ncu_ipc * busy_sms / (4.0 * sms) if ncu_ipc else None},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "plain_gpu": {"value": plain, "unit": UNIT,
                           "form": "one chain per launch, FP64 energy change, one sweep per launch, no graph"},

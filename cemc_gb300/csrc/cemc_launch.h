@@ -71,6 +71,7 @@ struct McLayout {
   // per-round trial records (two buffers, by round parity), kRoundSlots entries each
   size_t rec, rec_stride, rec_sa, rec_sb, rec_de, rec_ds, rec_acc, rec_la, rec_lb, rec_A, rec_B;
   size_t drow;  // [2][warps * tpw][n_eci] correlation-function changes of this CTA's trials
+  size_t cfp;   // spin form: per-lane sums of booked change rows [2][n_eci][32] (int32)
   size_t ftab, geos;  // table form
   size_t draws, rows;
   size_t warp0, warp_stride, warp_part;
@@ -151,6 +152,8 @@ __host__ __device__ inline McLayout mc_layout(const DevGeo &g, int warps, int mo
   o = align16(o + 2 * L.rec_stride);
   L.drow = o;  // two buffers (round parity) of [warps * tpw][n_eci] (none in the table form)
   if (!table) o = align16(o + 2 * (size_t)rsize * warps * tpw * K);
+  L.cfp = o;
+  if (spin) o = align16(o + 4 * 2 * 32 * K);
   L.ftab = o;  // table form: per-chain pattern tables F, then the geometry list
   if (table) o = align16(o + (size_t)rsize * g.tab_len);
   L.geos = o;

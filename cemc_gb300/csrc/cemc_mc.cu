@@ -359,6 +359,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   if (!TAB)
     for (int i = tid; i < 2 * TPW * W * n_eci; i += blockDim.x)
       drow[i] = (DT)0;  // the spin path writes only the entries of cluster and singlet ECIs
+  if (SPIN)
+    for (int i = tid; i < 2 * 32 * n_eci; i += blockDim.x) reinterpret_cast<int32_t *>(smem + L.cfp)[i] = 0;
   if (TAB) {
     // this chain's pattern tables F(old, new, member species), in FP64 then rounded to R
     const int S = g.n_sym;
@@ -647,10 +649,43 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     if constexpr (SPIN) return acc_from<A>((double)c);
     else return c;
   };
+  // Spin form: the change rows are integers, so lane j adds the row of its own
+  // slot own_lo + j to lane-private int32 sums cfp[k][j] (no exchange between
+  // lanes per round), folded into the 64-bit sums every kCfFoldRounds rounds and
+  // at the end.  A row entry is 2 P with |P| <= 64 pair terms + 32 x 63 multi-site
+  // terms, so 32 lanes x 4096 rounds of it stay below 2^31.
+  constexpr uint32_t kCfFoldRounds = 4096;
+  int32_t *cfp = reinterpret_cast<int32_t *>(smem + L.cfp) + (size_t)(CL == 1 ? bq : 0) * n_eci * 32;
+  auto cf_fold = [&]() {
+    if constexpr (SPIN) {
+      for (int k = 0; k < n_eci; ++k) {
+        const int tot = __reduce_add_sync(kFull, cfp[32 * k + lane]);
+        cfp[32 * k + lane] = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if ((k >> 5) == i && (k & 31) == lane) cfr[i] += (long long)tot;
+      }
+    }
+  };
   auto book_cf = [&](const unsigned char *rec, const DT *dbuf, int ks) {
     const int8_t *r_acc = reinterpret_cast<const int8_t *>(rec + L.rec_acc);
     const int hi = ks < own_hi ? ks : own_hi;
     const int j = own_lo + lane;
+    if constexpr (SPIN) {
+      if (j < hi && r_acc[j]) {
+        const DT *D = dbuf + (size_t)(j - (CL == 2 ? own_lo : 0)) * n_eci;
+        for (int k0 = 0; k0 < n_eci; k0 += 16) {
+          int32_t d[16];  // the row first: loads that no store of cfp has to precede
+#pragma unroll
+          for (int i = 0; i < 16; ++i) d[i] = k0 + i < n_eci ? (int32_t)D[k0 + i] : 0;
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (k0 + i < n_eci) cfp[32 * (k0 + i) + lane] += d[i];
+        }
+      }
+      __syncwarp();
+      return;
+    }
     unsigned am = __ballot_sync(kFull, j < hi && r_acc[j]);
     while (am) {
       const int jj = own_lo + __ffs(am) - 1;
@@ -1122,12 +1157,15 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
       if (round > 1)
         book(rec0 + (size_t)((round - 1) & 1) * L.rec_stride, drow + (size_t)((round - 1) & 1) * TPW * W * n_eci,
              ks_prev, t0 - (uint64_t)ks_prev);
+      if constexpr (SPIN)
+        if ((round & (kCfFoldRounds - 1)) == 0) cf_fold();
       int ks;
       if (!end_round(round, t0, active, ks)) break;
       ks_prev = ks;
       t0 += (uint64_t)ks;
       ++round;
     }
+    if constexpr (SPIN) cf_fold();
     for (int i = 0; i < 4; ++i) {
       const int k = lane + 32 * i;
       if (k < n_eci) cfb[k] = cf_sum_out(cfr[i]);

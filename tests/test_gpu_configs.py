@@ -85,7 +85,7 @@ def test_gpu_headline_sgc64_matches_oracle(E, oracle_mod):
     runner.step()
     runner.synchronize()
     runner.cb.check_status()
-    assert runner.cb.last_kernel in (E.KERNEL_SPIN_HALFWARP, E.KERNEL_SPIN, E.KERNEL_FIELD)
+    assert runner.cb.last_kernel in (E.KERNEL_SPIN_QUARTER, E.KERNEL_SPIN_HALFWARP, E.KERNEL_SPIN, E.KERNEL_FIELD)
     orc = oracle_mod.Oracle(m)
     n = m.n_sites
     occ_gpu = runner.cb.occ.cpu().numpy()
