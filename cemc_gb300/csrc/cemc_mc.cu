@@ -215,6 +215,14 @@ __device__ __forceinline__ void st_peer(uint32_t a, double v) {
 __device__ __forceinline__ void st_peer(uint32_t a, uint64_t v) {
   asm volatile("st.shared::cluster.u64 [%0], %1;\n" ::"r"(a), "l"(v) : "memory");
 }
+// Conflict stamp into this CTA's shared table when `on`: a predicated reduction
+// with no returned value and no branch, so a lane's stamps issue back to back.
+__device__ __forceinline__ void red_max_shared_if(const uint32_t *p, bool on, uint32_t v) {
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  asm volatile("{\n.reg .pred q;\nsetp.ne.u32 q, %2, 0;\n@q red.shared.max.u32 [%0], %1;\n}\n" ::"r"(a), "r"(v),
+               "r"((uint32_t)on)
+               : "memory");
+}
 __device__ __forceinline__ void red_max_peer(uint32_t a, uint32_t v) {
   asm volatile("red.shared::cluster.max.u32 [%0], %1;\n" ::"r"(a), "r"(v) : "memory");
 }
@@ -855,12 +863,27 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           // odd-parity counts of each multi-site cluster ECI: one reduction serves every
           // lane group (group h's count in bits FB h .. FB h + FB - 1; at most 255 when FB = 8)
           int my_odd = 0;
-          for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
-            const int k = __ffs(mm) - 1;
-            const int sl = k - sp_first;
-            const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
-            const uint32_t tot = __reduce_add_sync(kFull, v << (FB * h));
-            if (hl == k) my_odd = (int)((tot >> (FB * h)) & ((1u << FB) - 1u));
+          if constexpr (TPW == 4) {
+            // at most 8 cluster ECIs of at most 255 terms: every ECI's count in an 8-bit field
+            // of one 64-bit word, summed over the trial's 8 lanes by a butterfly (each partial
+            // sum is part of a total <= 255, so no field carries into the next)
+            uint64_t wsum = 0;
+#pragma unroll
+            for (int sl = 0; sl < 5; ++sl)
+              if (sp_first + sl < 8) wsum |= (uint64_t)((pa >> (6 * sl)) & 63u) << (8 * (sp_first + sl));
+            if (sp_multi) {
+#pragma unroll
+              for (int o = 1; o < LW; o <<= 1) wsum += __shfl_xor_sync(kFull, wsum, o);
+            }
+            my_odd = (int)((wsum >> (8 * (hl & 7))) & 255u);
+          } else {
+            for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+              const int k = __ffs(mm) - 1;
+              const int sl = k - sp_first;
+              const uint32_t v = (sl >= 0 && sl < 5) ? ((pa >> (6 * sl)) & 63u) : 0u;
+              const uint32_t tot = __reduce_add_sync(kFull, v << (FB * h));
+              if (hl == k) my_odd = (int)((tot >> (FB * h)) & ((1u << FB) - 1u));
+            }
           }
           const int delta = occ_a_bit ? 2 : -2;
           DT *Dh = dbuf + (size_t)(TPW * warp + h) * n_eci;  // this CTA's change row of the trial
@@ -887,8 +910,12 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             put(&r_ds[gh], (R)delta);  // the singlet change (one decoration)
           }
           acc = __shfl_sync(kFull, acc, LW * h);
-          if (acc) {
-            const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
+          const uint32_t mark = (round << 6) | (uint32_t)(63 - gh);
+          if (CL == 1 && !gst) {
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) red_max_shared_if(&tab[(uint32_t)nbr[j] & hmask], acc && nbr[j] >= 0, mark);
+            red_max_shared_if(&tab[(uint32_t)sa & hmask], acc && hl == 0, mark);
+          } else if (acc) {
 #pragma unroll
             for (int j = 0; j < NJ; ++j)
               if (nbr[j] >= 0) {
