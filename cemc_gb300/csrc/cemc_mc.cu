@@ -936,8 +936,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         if (active && t < t_end) {
           const uint32_t slot = (uint32_t)t & rmask;
           const Draw dr = draws[slot];
-          int sa, sb = -1, na, A_ = 0, B_ = 0, old_a = 0;
-          int nbra[4], nbrb[4] = {-1, -1, -1, -1};
+          int sa = 0, sb = -1, na = 0, A_ = 0, B_ = 0, old_a = 0;
+          int nbra[4] = {-1, -1, -1, -1}, nbrb[4] = {-1, -1, -1, -1};
           uint32_t ua, ub;
           uint32_t occ_a_bit = 0, wa_lo = 0, wa_hi = 0, wb_lo = 0, wb_hi = 0;  // spin path
           // Move constraints: an illegal proposal is redrawn, proposal k of trial t from
@@ -1123,7 +1123,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             }
           }
           acc = __shfl_sync(kFull, acc, 0);
-          if (acc) {
+          if (CL == 1 && !gst) {
+            const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              red_max_shared_if(&tab[(uint32_t)nbra[q] & hmask], acc && nbra[q] >= 0, mark);
+              if (SWAP) red_max_shared_if(&tab[(uint32_t)nbrb[q] & hmask], acc && nbrb[q] >= 0, mark);
+            }
+            red_max_shared_if(&tab[(uint32_t)sa & hmask], acc && lane == 0, mark);
+            if (SWAP) red_max_shared_if(&tab[(uint32_t)sb & hmask], acc && lane == 0, mark);
+          } else if (acc) {
             const uint32_t mark = (round << 6) | (uint32_t)(63 - gidx);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {

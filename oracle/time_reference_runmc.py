@@ -11,7 +11,7 @@ small calculator exposing the methods the drivers call on the reference's
 ``CE`` (cemc/ce_calculator.py:319-395).  Runs only where the reference tree is
 present.
 
-    python oracle/time_reference_runmc.py [--steps 20000]
+    CEMC_REFERENCE=<reference tree> python oracle/time_reference_runmc.py [--steps 20000]
 """
 from __future__ import annotations
 
@@ -27,7 +27,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF = os.environ.get("CEMC_REFERENCE", "/root/reference")
+REF = os.environ.get("CEMC_REFERENCE", "")
+if not os.path.isdir(os.path.join(REF, "cemc")):
+    sys.exit("set CEMC_REFERENCE to the reference source tree (it holds cemc/ and cpp/)")
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
 

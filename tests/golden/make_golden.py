@@ -19,7 +19,7 @@ Run in a checkout where the reference has been compiled by
 The fixtures then pin the oracle (CPU tests) and the GPU path (GPU tests) to
 the reference on machines without the reference tree.
 
-    python tests/golden/make_golden.py
+    CEMC_REFERENCE=<reference tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -177,7 +177,9 @@ def build_constraint_verdicts():
     """
     import importlib.util
     import types
-    ref = os.environ.get("CEMC_REFERENCE", "/root/reference")
+    ref = os.environ.get("CEMC_REFERENCE", "")
+    if not os.path.isdir(os.path.join(ref, "cemc")):
+        raise SystemExit("set CEMC_REFERENCE to the reference source tree (it holds cemc/ and cpp/)")
 
     def load(name, rel):
         spec = importlib.util.spec_from_file_location(name, os.path.join(ref, rel))
