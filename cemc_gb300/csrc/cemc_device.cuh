@@ -220,6 +220,28 @@ __device__ __forceinline__ int metropolis(R de, uint32_t ua, uint32_t ub, double
   return cemc_u01_53(ua, ub) <= exp(-(double)de / kT);
 }
 
+// The same test with the uniform's parts precomputed (by the fetcher, off the
+// evaluating warps' path): lnu = __logf(u) and mu = 1e-4 + 1e-8 / u for
+// u = ua * 2^-32.  The margin can differ from metropolis()'s in its last bit,
+// which only moves a trial between the single-precision test and the exact one.
+// `uw` points at the uniform's two words, read only inside the margin.
+template <typename R>
+__device__ __forceinline__ int metropolis_pre(R de, float lnu, float mu, const uint32_t *uw, double kT,
+                                              float inv_kT) {
+  if (de < (R)0) return 1;
+  const float x = (float)de * inv_kT;
+  const float y = lnu + x;
+  const float margin = mu + 1e-6f * x;  // u == 0 gives an infinite margin
+  if (y < -margin) return 1;
+  if (y > margin) return 0;
+  return cemc_u01_53(uw[0], uw[1]) <= exp(-(double)de / kT);
+}
+__device__ __forceinline__ void metropolis_parts(uint32_t ua, float &lnu, float &mu) {
+  const float uf = (float)ua * 2.3283064e-10f;  // a * 2^-32
+  lnu = __logf(uf);
+  mu = 1e-4f + 1e-8f / uf;
+}
+
 // Two-state acceptance of waste recycling (Frenkel, PNAS 101, 17571 (2004);
 // montecarlo.py:937-948): the reference draws the next state from the weights
 // exp(-E / kT) of the current and the proposed state, i.e. it accepts when

@@ -515,6 +515,16 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
         }
       } else {
         d.x0 = d.x1 = 0;
+        if constexpr (TPW >= 2) {
+          // unconstrained flips: the acceptance test's parts of the uniform in w2, w3 (read with
+          // the site), the uniform's words in x0, x1 (read only by the exact fallback)
+          float lnu, mu;
+          metropolis_parts(d.w2, lnu, mu);
+          d.x0 = d.w2;
+          d.x1 = d.w3;
+          d.w2 = __float_as_uint(lnu);
+          d.w3 = __float_as_uint(mu);
+        }
         // the flipped site: uniform over the movable sites (all sites without a background)
         d.site = g.n_movable == N ? (int)cemc_below(w0.v[0], (uint32_t)N)
                                   : g.movable[cemc_below(w0.v[0], (uint32_t)g.n_movable)];
@@ -829,15 +839,15 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           const bool has = t < t_end;  // the last groups of the last warp may have no trial
           const uint32_t slot = (uint32_t)t & rmask;
           int sa = 0, na = 0, oa = 0;
-          uint32_t ua = 0, ub = 0;
+          float lnu = 0.f, mu = 0.f;
           if (has) {
-            const Draw dr = draws[slot];
-            sa = dr.site;
+            const uint4 dr = *reinterpret_cast<const uint4 *>(&draws[slot]);  // site, w1, w2, w3
+            sa = (int)dr.x;
             oa = occ[sa];
-            const int k = (int)cemc_below(dr.w1, (uint32_t)(g.n_sym - 1));
+            const int k = (int)cemc_below(dr.y, (uint32_t)(g.n_sym - 1));
             na = k + (k >= oa);
-            ua = dr.w2;
-            ub = dr.w3;
+            lnu = __uint_as_float(dr.z);
+            mu = __uint_as_float(dr.w);
           }
           const uint32_t occ_a_bit = (uint32_t)oa ^ xorv;
           // spin word of the neighbour row: bit c = column c, from NJ ballots of LW
@@ -902,7 +912,7 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
           const R de = (R)delta * sum;
           int acc = 0;
           if (hl == 0 && has) {
-            acc = metropolis<R>(de, ua, ub, kT, inv_kT);
+            acc = metropolis_pre<R>(de, lnu, mu, &draws[slot].x0, kT, inv_kT);
             put(&r_sa[gh], (int32_t)sa);
             put(&r_sb[gh], (int32_t)na);
             put(&r_acc[gh], (int8_t)acc);
