@@ -50,6 +50,12 @@ __host__ __device__ inline int round_trials(int cl, int warps, int tpw) { return
 __host__ __device__ inline int n_bookers(int cl, int warps, int tpw) {
   return (cl == 1 && round_trials(cl, warps, tpw) > 32) ? 2 : 1;
 }
+// Largest CTA of a kernel build, its launch bound: forms whose CTAs stay under 640 threads
+// (four trials per warp; two per warp in a CTA pair: at most 16 evaluating warps and three
+// helpers) leave the compiler 102 registers a thread instead of 64.
+__host__ __device__ constexpr int mc_max_threads(int tpw, int cl) {
+  return (tpw == 4 || (tpw == 2 && cl == 2)) ? 640 : 1024;
+}
 // Evaluating warps per CTA that fit next to the helpers in 1024 threads.
 __host__ __device__ inline int max_eval_warps(int cl, int tpw) {
   if (tpw == 4) return kRoundSlots / 4;                 // four trials per warp, one CTA per chain

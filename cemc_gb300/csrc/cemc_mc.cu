@@ -240,7 +240,7 @@ __device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
 // CONS: this build runs the move-constraint redraw loop and the first-move acceptance (one
 // trial per warp, one CTA per chain); unconstrained launches take builds without them.
 template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS>
-__global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
+__global__ void __launch_bounds__(mc_max_threads(TPW, CL), 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
   constexpr bool SPIN = (FORM == kFormSpin), TAB = (FORM == kFormTable);
@@ -753,6 +753,10 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
   SpinEci sp_e{};
   R sp_coef = (R)0;
   unsigned sp_multi = 0;  // cluster ECIs with multi-site terms
+  // Flips at one or two trials per warp: the odd-term counts of all multi-site ECIs by one
+  // packed butterfly (odd_counts_packed) when each has at most 255 terms and their 8-bit
+  // fields fit one 64-bit word; else one reduction per ECI.
+  bool sp_pk = false;
   int sp_tlo = 0, sp_thi = 0, sp_first = 0;  // this lane's range of multi-site terms
   if (SPIN) {
     // two trials per warp: lane l works for trial l / 16 on cluster ECI (and term range) l % 16
@@ -767,7 +771,36 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
     }
     sp_multi = __ballot_sync(kFull, el < sd.n_cl && sp_e.n_multi > 0);
     if constexpr (TPW >= 2) sp_multi &= (1u << (32 / TPW)) - 1u;
+    // (not for swaps: their second site's fields cost the FP64 swap build registers it spills)
+    if constexpr (TPW <= 2 && !SWAP)
+      sp_pk = __popc(sp_multi) <= 8 && __all_sync(kFull, el >= sd.n_cl || sp_e.n_multi <= 255);
   }
+  // Lane group of LW lanes: counters pa (and pb, the second site of a swap) of this lane's
+  // terms, 6 bits per cluster ECI from sp_first on; the group's total for ECI el of each
+  // multi-site ECI, in field (its rank among the multi-site ECIs) of one 64-bit word summed
+  // by a butterfly.  Every partial sum is part of a total <= 255, so no field carries.
+  auto odd_counts_packed = [&](uint32_t pa, uint32_t pb, int el, auto lw_tag) -> int {
+    constexpr int LWP = decltype(lw_tag)::value;
+    uint64_t wsum = 0;
+#pragma unroll
+    for (int sl = 0; sl < 5; ++sl) {
+      const int k = sp_first + sl;
+      if (k < 32 && ((sp_multi >> k) & 1u)) {
+        const int m = __popc(sp_multi & ((1u << k) - 1u));
+        wsum += (uint64_t)((pa >> (6 * sl)) & 63u) << (8 * m);
+        if (SWAP) wsum += (uint64_t)((pb >> (6 * sl)) & 63u) << (8 * (m + 4));
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < LWP; o <<= 1) wsum += __shfl_xor_sync(kFull, wsum, o);
+    int odd = 0;
+    if ((sp_multi >> el) & 1u) {
+      const int m = __popc(sp_multi & ((1u << el) - 1u));
+      odd = (int)((wsum >> (8 * m)) & 255u);
+      if (SWAP) odd -= (int)((wsum >> (8 * (m + 4))) & 255u);
+    }
+    return odd;
+  };
 
   // One round: every warp, whatever its role, meets the round barrier once and
   // computes the same committed prefix `ks`, so the role loops below run in
@@ -886,6 +919,8 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
               for (int o = 1; o < LW; o <<= 1) wsum += __shfl_xor_sync(kFull, wsum, o);
             }
             my_odd = (int)((wsum >> (8 * (hl & 7))) & 255u);
+          } else if (sp_pk) {
+            my_odd = odd_counts_packed(pa, 0u, hl, std::integral_constant<int, LW>{});
           } else {
             for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
               const int k = __ffs(mm) - 1;
@@ -1075,13 +1110,17 @@ __global__ void __launch_bounds__(1024, 1) mc_kernel(DevGeo g, RunArgs a, SpinDe
             const uint32_t pa = spin_lane_parities<false>(sp_terms, sp_tlo, sp_thi, wa_lo, wa_hi);
             const uint32_t pb = SWAP ? spin_lane_parities<false>(sp_terms, sp_tlo, sp_thi, wb_lo, wb_hi) : 0u;
             int my_odd = 0;
-            for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
-              const int k = __ffs(mm) - 1;
-              const int sl = k - first;
-              int v = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
-              if (SWAP) v -= (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
-              const int odd = __reduce_add_sync(kFull, v);
-              if (lane == k) my_odd = odd;
+            if (sp_pk) {
+              my_odd = odd_counts_packed(pa, pb, lane, std::integral_constant<int, 32>{});
+            } else {
+              for (unsigned mm = sp_multi; mm; mm &= mm - 1) {
+                const int k = __ffs(mm) - 1;
+                const int sl = k - first;
+                int v = (sl >= 0 && sl < 5) ? (int)((pa >> (6 * sl)) & 63u) : 0;
+                if (SWAP) v -= (sl >= 0 && sl < 5) ? (int)((pb >> (6 * sl)) & 63u) : 0;
+                const int odd = __reduce_add_sync(kFull, v);
+                if (lane == k) my_odd = odd;
+              }
             }
             int P = 0;
             if (lane < sd.n_cl) {
@@ -1317,6 +1356,7 @@ static unsigned block_threads(const RunArgs &a) {
 template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS = false>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
   auto k = mc_kernel<R, MOVE, FORM, CL, TPW, CONS>;
+  if (block_threads(a) > mc_max_threads(TPW, CL)) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
