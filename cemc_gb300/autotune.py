@@ -24,8 +24,8 @@ import torch
 
 from . import engine as E
 
-CANDIDATES = (4, 8, 16, 24, 30)          # warps per CTA, one CTA per chain
-PAIR_CANDIDATES = (8, 16, 24, 30)        # warps per CTA, cluster pairs
+CANDIDATES = (4, 8, 12, 16)              # warps per CTA, one CTA per chain
+PAIR_CANDIDATES = (8, 12, 16)            # warps per CTA, cluster pairs
 FIELD_CANDIDATES = (16, 28)              # worker warps of the local-field form
 QUARTER_CANDIDATES = (8, 12, 16)         # warps of the quarter-warp spin form (four flips per warp)
 _CACHE_PATH = os.environ.get("CEMC_AUTOTUNE_CACHE",

@@ -40,7 +40,7 @@ struct RunArgs {
   int cons;          // 1: the build with the constraint redraw loop and first-move acceptance (one CTA per chain)
 };
 
-constexpr int kMaxEval = 30;   // trial-evaluating warps per CTA; two or three more warps are helpers
+constexpr int kMaxEval = 16;   // trial-evaluating warps per CTA; two or three more warps are helpers
 constexpr int kRoundSlots = 64;  // trial records per round (trials per round <= 60)
 constexpr int kPrefetchRounds = 3;  // the fetcher draws this many rounds of trials ahead
 
@@ -50,16 +50,14 @@ __host__ __device__ inline int round_trials(int cl, int warps, int tpw) { return
 __host__ __device__ inline int n_bookers(int cl, int warps, int tpw) {
   return (cl == 1 && round_trials(cl, warps, tpw) > 32) ? 2 : 1;
 }
-// Largest CTA of a kernel build, its launch bound: forms whose CTAs stay under 640 threads
-// (four trials per warp; two per warp in a CTA pair: at most 16 evaluating warps and three
-// helpers) leave the compiler 102 registers a thread instead of 64.
-__host__ __device__ constexpr int mc_max_threads(int tpw, int cl) {
-  return (tpw == 4 || (tpw == 2 && cl == 2)) ? 640 : 1024;
-}
-// Evaluating warps per CTA that fit next to the helpers in 1024 threads.
+// Launch bound of every kernel build: at most 16 evaluating warps and three helpers
+// (608 threads), which leaves the compiler 102 registers a thread instead of the 64 of a
+// 1024-thread bound (wider CTAs were never the faster shape; the bound is worth 2-6 %).
+constexpr int kMcMaxThreads = 640;
+// Evaluating warps per CTA (larger requests are clamped).
 __host__ __device__ inline int max_eval_warps(int cl, int tpw) {
-  if (tpw == 4) return kRoundSlots / 4;                 // four trials per warp, one CTA per chain
-  if (tpw == 2) return cl == 1 ? 29 : kRoundSlots / 4;  // a pair of half-warp CTAs: 4 trials per warp index
+  (void)cl;
+  (void)tpw;
   return kMaxEval;
 }
 // Ring size (log2): more than kPrefetchRounds rounds of trials.

@@ -240,7 +240,7 @@ __device__ __forceinline__ double ld_peer_acc(const df64 *p, unsigned rank) {
 // CONS: this build runs the move-constraint redraw loop and the first-move acceptance (one
 // trial per warp, one CTA per chain); unconstrained launches take builds without them.
 template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS>
-__global__ void __launch_bounds__(mc_max_threads(TPW, CL), 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
+__global__ void __launch_bounds__(kMcMaxThreads, 1) mc_kernel(DevGeo g, RunArgs a, SpinDev sd) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SWAP = (MOVE == CEMC_MOVE_SWAP);
   constexpr bool SPIN = (FORM == kFormSpin), TAB = (FORM == kFormTable);
@@ -1356,7 +1356,7 @@ static unsigned block_threads(const RunArgs &a) {
 template <typename R, int MOVE, int FORM, int CL, int TPW, bool CONS = false>
 static cudaError_t launch_t(const DevGeo &g, const RunArgs &a, size_t smem, cudaStream_t st, const SpinDev &sd) {
   auto k = mc_kernel<R, MOVE, FORM, CL, TPW, CONS>;
-  if (block_threads(a) > mc_max_threads(TPW, CL)) return cudaErrorInvalidConfiguration;
+  if (block_threads(a) > kMcMaxThreads) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};

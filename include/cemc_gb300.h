@@ -138,7 +138,8 @@ typedef struct {
   int32_t n_chains;
   int32_t move;        /* CEMC_MOVE_* */
   int32_t precision;   /* CEMC_PREC_* */
-  int32_t warps;       /* evaluating warps per CTA (trials per round = warps x CTAs per chain); 0 = default */
+  int32_t warps;       /* evaluating warps per CTA, at most 16, larger values are clamped (trials per round =
+                          warps x trials per warp x CTAs per chain); 0 = default */
   uint64_t seed;
   uint64_t n_trials;   /* trials per chain in this launch */
   int8_t *occ;

@@ -270,7 +270,7 @@ def test_fp32_drift_and_recompute_at_benchmark_size(torch_cuda):
     Ts, mus = sgc_grid()
     ev = fold_chemical_potential(m, m.eci_vector(eci), mus)
     cb = E.ChainBatch(geo, occ, ev, KB * Ts, E.MOVE_FLIP, seed=3)
-    cb.run(3 * m.n_sites, precision=E.PREC_F32, warps=24)
+    cb.run(3 * m.n_sites, precision=E.PREC_F32, warps=16)
     torch.cuda.synchronize()
     cf_inc, e_inc = cb.cf.cpu().numpy().copy(), cb.energy.cpu().numpy().copy()
     cb.recompute()

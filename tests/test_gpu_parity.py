@@ -82,7 +82,7 @@ CLUSTERS = [1, 2]  # CTAs per chain
 
 @pytest.mark.parametrize("cluster", CLUSTERS)
 @pytest.mark.parametrize("kernel", KERNELS)
-@pytest.mark.parametrize("warps", [1, 16, 30])
+@pytest.mark.parametrize("warps", [1, 9, 16])
 @pytest.mark.parametrize("case", golden_cases())
 def test_gpu_replays_reference_fixture_fp64(case, warps, kernel, cluster, E):
     g = load_golden(case)
@@ -435,7 +435,7 @@ def test_gpu_global_stamp_tables_match_oracle(move, E, oracle_mod, monkeypatch):
     for global_tables in (True, False):
         monkeypatch.setattr(E, "STAMP_GLOBAL_SITES", 0 if global_tables else 1 << 30)
         cb = E.ChainBatch(geo, occ[None], ev, kT, move, seed=31)
-        _, acc, _ = cb.run(n, precision=E.PREC_F64, warps=30, trace=True, cluster=1)
+        _, acc, _ = cb.run(n, precision=E.PREC_F64, warps=16, trace=True, cluster=1)
         _sync()
         cb.check_status()
         assert (cb._stamp_buf is not None) == global_tables
