@@ -175,7 +175,7 @@ def measured_peak():
 # Per kernel form (CEMC_KERNEL_* id): (DRAM bytes per launch, IPC per busy SM, launch captured).
 NCU_FIGURES = {3: (4820224.0, 2.23, "one 10-sweep launch"),
                5: (4820992.0, 2.31, "one 2-sweep launch (traffic does not grow with sweeps)"),
-               6: (4837120.0, 1.73, "one 10-sweep launch")}
+               6: (4830976.0, 1.62, "one 10-sweep launch")}
 NCU_SOURCE = "ncu capture of the same kernel and workload: "
 KERNEL_NAMES = {1: "generic", 2: "spin", 3: "spin half-warp", 4: "table", 5: "local field", 6: "spin quarter-warp"}
 KERNEL_CHOICES = {"auto": 0, "generic": 1, "spin": 2, "half": 3, "table": 4, "field": 5, "quarter": 6}
